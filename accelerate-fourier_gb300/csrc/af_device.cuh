@@ -1,0 +1,304 @@
+// af_device.cuh -- device-side building blocks of libaf: descriptors shared by
+// host and device, complex arithmetic, fast integer division, twiddle lookup
+// and the radix-R butterflies used by the shared-memory Stockham engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define AF_MAXP 14      // max Stockham passes per FFT phase
+#define AF_MAXPH 2      // max FFT phases in one tile program
+#define AF_HD __host__ __device__ __forceinline__
+
+typedef long long i64;
+
+// ---------------------------------------------------------------- fast divide
+// q = floor(x / d) for 0 <= x < 2^31 via a 32-bit magic multiply.
+struct FastDiv {
+  unsigned d, m, s;
+};
+static inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  if (d <= 1) { f.m = 0; f.s = 0; return f; }
+  unsigned s = 0;
+  while ((1ull << s) < d) ++s;
+  f.s = s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
+  return f.d <= 1 ? x : ((__umulhi(x, f.m) + x) >> f.s);
+}
+
+// ---------------------------------------------------------------- complex ops
+AF_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+AF_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+AF_HD float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+AF_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+AF_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+// multiply by sign*i  (sign = +-1):  (sign*i)(x+iy) = sign*(-y + ix)
+AF_HD float2 mul_si(float2 a, float sign) { return make_float2(-sign * a.y, sign * a.x); }
+
+// ---------------------------------------------------------------- descriptors
+// One Stockham pass of radix R over a phase of length n: the pass reads
+// element i + j*(n/R) and writes (i-k)*R + k + j*p with k = i mod p.
+struct PassDesc {
+  int R;
+  int p;
+  int tw_stride;   // n / (p*R): exponent step of the twiddle table for this pass
+  FastDiv nb_div;  // n / R  (butterflies per line)
+  FastDiv p_div;   // p
+};
+
+// One FFT phase: G transforms per CTA, each holding `lcnt` lines of length n.
+// Line r of transform t starts at shared position t*LS + r*ls and its
+// elements are es apart (positions before bank padding).
+struct FftPhase {
+  int n, npass, ls, es, lcnt;
+  float sign;
+  int tw_off;      // offset of this phase's tables in the shared table area
+  int twS_log2;    // two-level table split S = 1<<twS_log2 (lo table S, hi table H)
+  FastDiv lcnt_div;
+  PassDesc pass[AF_MAXP];
+};
+
+// Global-memory view of one side (input or output) of a tile program.
+// A tile "line" l of a launch is split as hi = l / lo_count, lo = l % lo_count,
+// and element e of that line lives at  hi*s_hi + lo*s_lo + e*s_e  (complex
+// units).  Planar layout uses re/im float planes with the same indexing.
+struct IoDesc {
+  float2* c;        // interleaved base, or NULL
+  float* re;        // planar re plane (when c == NULL)
+  float* im;        // planar im plane
+  i64 s_e, s_lo, s_hi;
+  FastDiv lo_div;
+  int line_fast;    // 1: consecutive threads walk lines (strided element access)
+};
+
+enum TileKind {
+  TILE_PLAIN = 0,     // load -> FFT -> store
+  TILE_GT = 1,        // Good-Thomas: CRT load -> FFT_n rows -> FFT_m cols -> CRT store
+  TILE_RADER = 2,     // Rader: dlog gather -> FFT(+1) -> *zs -> FFT(-1) -> dlog scatter + x0
+  TILE_BLUESTEIN = 3  // Bluestein: chirp*x, pad -> FFT(+1) -> *spec -> FFT(-1) -> chirp*, take N
+};
+
+struct TileDesc {
+  int kind;
+  int nlen;          // logical transform length N seen through in/out
+  int G;             // transforms ("lines" of the launch) per CTA
+  int nlines;        // total lines of the launch
+  int LS;            // shared-memory stride between transforms (unpadded units)
+  int slen;          // elements per transform held in shared memory (M for conv tiles)
+  int tw_total;      // float2 table entries staged in shared memory
+  const float2* tw_src;  // table source (device)
+  FftPhase ph[AF_MAXPH];
+  int nph;
+  FastDiv N_div, S_div, G_div;  // nlen, slen, G
+  IoDesc in, out;
+  float scale;       // multiplies every stored element
+  // four-step post twiddle: element e of a line with column c = lo*ptw_col_mul
+  // is multiplied by W_N^(c*e) (two-level table: S lo entries then hi entries)
+  const float2* ptw;
+  int ptwS_log2;
+  i64 ptwN;
+  int ptw_col_mul;
+  float ptw_sign;
+  // Good-Thomas grid m x n: logical input i sits at ((i*gt_cm) mod m)*n + (i*gt_cn) mod n
+  int gt_n, gt_m;
+  i64 gt_cm, gt_cn;
+  // Rader: dlog[r-1] = log_g(r) for r = 1..p-1
+  const int* dlog;
+  // Bluestein chirp (N entries); conv spectrum (slen entries): Rader zs / chirp spectrum
+  const float2* vec_a;
+  const float2* vec_b;
+};
+
+// ---------------------------------------------------------------- smem layout
+// One padding slot every 16 float2 keeps strided Stockham writes bank friendly.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+
+// ---------------------------------------------------------------- twiddles
+// Tables hold the forward root: tab[t] = exp(-2*pi*i*t/n), as two levels
+// lo[t & (S-1)] * hi[t >> log2 S].  sign > 0 conjugates.
+__device__ __forceinline__ float2 tw_lookup(const float2* tab, int S_log2, int t, float sign) {
+  float2 lo = tab[t & ((1 << S_log2) - 1)];
+  float2 hi = tab[(1 << S_log2) + (t >> S_log2)];
+  float2 w = cmul(hi, lo);
+  w.y *= -sign;  // forward (sign=-1) keeps the stored root
+  return w;
+}
+
+// ---------------------------------------------------------------- butterflies
+// In-register DFT of R points, y_k = sum_j u_j exp(sign*2*pi*i*j*k/R).
+template <int R> struct Dft;
+
+template <> struct Dft<2> {
+  static __device__ __forceinline__ void run(float2* u, float, const float2*, int, int) {
+    float2 a = u[0], b = u[1];
+    u[0] = cadd(a, b);
+    u[1] = csub(a, b);
+  }
+};
+
+__device__ __forceinline__ void dft4(float2& u0, float2& u1, float2& u2, float2& u3, float sign) {
+  float2 t0 = cadd(u0, u2), t1 = csub(u0, u2);
+  float2 t2 = cadd(u1, u3), t3 = mul_si(csub(u1, u3), sign);
+  u0 = cadd(t0, t2);
+  u2 = csub(t0, t2);
+  u1 = cadd(t1, t3);
+  u3 = csub(t1, t3);
+}
+
+template <> struct Dft<4> {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+    dft4(u[0], u[1], u[2], u[3], sign);
+  }
+};
+
+#define AF_R2 0.70710678118654752440f
+#define AF_C8 0.92387953251128675613f
+#define AF_S8 0.38268343236508977173f
+
+// multiply by w8^m = exp(sign*2*pi*i*m/8)
+__device__ __forceinline__ float2 mul_w8(float2 a, int m, float sign) {
+  switch (m & 7) {
+    case 0: return a;
+    case 1: return cmul(a, make_float2(AF_R2, sign * AF_R2));
+    case 2: return mul_si(a, sign);
+    case 3: return cmul(a, make_float2(-AF_R2, sign * AF_R2));
+    case 4: return make_float2(-a.x, -a.y);
+    case 5: return cmul(a, make_float2(-AF_R2, -sign * AF_R2));
+    case 6: return mul_si(a, -sign);
+    default: return cmul(a, make_float2(AF_R2, -sign * AF_R2));
+  }
+}
+
+template <> struct Dft<8> {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+    float2 a[4], b[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      a[j] = cadd(u[j], u[j + 4]);
+      b[j] = mul_w8(csub(u[j], u[j + 4]), j, sign);
+    }
+    dft4(a[0], a[1], a[2], a[3], sign);
+    dft4(b[0], b[1], b[2], b[3], sign);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { u[2 * k] = a[k]; u[2 * k + 1] = b[k]; }
+  }
+};
+
+// multiply by w16^m, m in 0..9
+__device__ __forceinline__ float2 mul_w16(float2 a, int m, float sign) {
+  switch (m) {
+    case 0: return a;
+    case 1: return cmul(a, make_float2(AF_C8, sign * AF_S8));
+    case 2: return mul_w8(a, 1, sign);
+    case 3: return cmul(a, make_float2(AF_S8, sign * AF_C8));
+    case 4: return mul_w8(a, 2, sign);
+    case 6: return mul_w8(a, 3, sign);
+    case 9: return cmul(a, make_float2(-AF_C8, -sign * AF_S8));
+    default: return a;  // unused
+  }
+}
+
+template <> struct Dft<16> {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+    // 4 x 4: v_a = DFT4(u[a + 4m]); v_a[b] *= w16^(a b); y[b + 4c] = DFT4_a(v_a[b])
+#pragma unroll
+    for (int a = 0; a < 4; ++a) dft4(u[a], u[a + 4], u[a + 8], u[a + 12], sign);
+#pragma unroll
+    for (int a = 1; a < 4; ++a)
+#pragma unroll
+      for (int b = 1; b < 4; ++b) u[a + 4 * b] = mul_w16(u[a + 4 * b], a * b, sign);
+    float2 t[16];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      float2 x0 = u[0 + 4 * b], x1 = u[1 + 4 * b], x2 = u[2 + 4 * b], x3 = u[3 + 4 * b];
+      dft4(x0, x1, x2, x3, sign);
+      t[b] = x0; t[b + 4] = x1; t[b + 8] = x2; t[b + 12] = x3;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) u[i] = t[i];
+  }
+};
+
+template <> struct Dft<3> {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+    const float c = -0.5f, s = 0.86602540378443864676f * sign;
+    float2 t = cadd(u[1], u[2]);
+    float2 d = csub(u[1], u[2]);
+    float2 m = make_float2(fmaf(c, t.x, u[0].x), fmaf(c, t.y, u[0].y));
+    float2 r = make_float2(-s * d.y, s * d.x);
+    u[0] = cadd(u[0], t);
+    u[1] = cadd(m, r);
+    u[2] = csub(m, r);
+  }
+};
+
+template <> struct Dft<5> {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+    const float s1 = 0.95105651629515357212f * sign, s2 = 0.58778525229247312917f * sign;
+    float2 p1 = cadd(u[1], u[4]), m1 = csub(u[1], u[4]);
+    float2 p2 = cadd(u[2], u[3]), m2 = csub(u[2], u[3]);
+    float2 a1 = make_float2(u[0].x + c1 * p1.x + c2 * p2.x, u[0].y + c1 * p1.y + c2 * p2.y);
+    float2 a2 = make_float2(u[0].x + c2 * p1.x + c1 * p2.x, u[0].y + c2 * p1.y + c1 * p2.y);
+    // b = i*(s1 m1 + s2 m2), c = i*(s2 m1 - s1 m2)
+    float2 b1 = make_float2(-(s1 * m1.y + s2 * m2.y), s1 * m1.x + s2 * m2.x);
+    float2 b2 = make_float2(-(s2 * m1.y - s1 * m2.y), s2 * m1.x - s1 * m2.x);
+    u[0] = cadd(u[0], cadd(p1, p2));
+    u[1] = cadd(a1, b1);
+    u[4] = csub(a1, b1);
+    u[2] = cadd(a2, b2);
+    u[3] = csub(a2, b2);
+  }
+};
+
+// Odd prime radix (7, 11, 13): symmetric direct DFT; cos/sin of 2*pi*m/R come
+// from the phase's twiddle table (R divides the phase length n: W_n^(m n/R)).
+template <int R> struct DftOdd {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2* tab, int S_log2, int n) {
+    constexpr int h = (R - 1) / 2;
+    float cs[R], sn[R];
+    const int step = n / R;
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      float2 w = tw_lookup(tab, S_log2, m * step, -1.0f);  // exp(-2 pi i m/R)
+      cs[m] = w.x;
+      sn[m] = -w.y;  // sin(2 pi m / R)
+    }
+    float2 P[h + 1], M[h + 1];
+    float2 y0 = u[0];
+#pragma unroll
+    for (int j = 1; j <= h; ++j) {
+      P[j] = cadd(u[j], u[R - j]);
+      M[j] = csub(u[j], u[R - j]);
+      y0 = cadd(y0, P[j]);
+    }
+    float2 out[R];
+    out[0] = y0;
+#pragma unroll
+    for (int k = 1; k <= h; ++k) {
+      float2 a = u[0], b = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 1; j <= h; ++j) {
+        int m = (j * k) % R;
+        a.x = fmaf(cs[m], P[j].x, a.x);
+        a.y = fmaf(cs[m], P[j].y, a.y);
+        b.x = fmaf(sn[m], M[j].x, b.x);
+        b.y = fmaf(sn[m], M[j].y, b.y);
+      }
+      float2 ib = mul_si(b, sign);
+      out[k] = cadd(a, ib);
+      out[R - k] = csub(a, ib);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) u[k] = out[k];
+  }
+};
+template <> struct Dft<7> : DftOdd<7> {};
+template <> struct Dft<11> : DftOdd<11> {};
+template <> struct Dft<13> : DftOdd<13> {};

@@ -1,0 +1,117 @@
+// af_host.h -- host-side structures of libaf: plan resources, launch
+// programs, and the plan object behind the C ABI's af_plan handle.
+#pragma once
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/af.h"
+#include "af_internal.h"
+#include "af_plan.h"
+
+namespace af {
+
+struct AfError : std::runtime_error {
+  af_status code;
+  AfError(af_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2 };
+
+// A batch of lines: line l = hi * lo_cnt + lo, element e at
+// off + hi*s_hi + lo*s_lo + e*s_e in buffer `buf` (complex units).
+struct View {
+  int buf = BUF_WS;
+  i64 off = 0;
+  i64 s_e = 1, s_lo = 0, s_hi = 0, lo_cnt = 1;
+  static View rows(int buf, i64 off, i64 n, i64 lines) {
+    View v;
+    v.buf = buf;
+    v.off = off;
+    v.s_e = 1;
+    v.s_lo = n;
+    v.s_hi = 0;
+    v.lo_cnt = lines < 1 ? 1 : lines;
+    return v;
+  }
+};
+
+enum StepType { STEP_TILE = 0, STEP_MAP = 1 };
+
+struct Step {
+  int type = STEP_TILE;
+  TileDesc td;
+  int threads = 256;
+  MapDesc md;
+  View vin, vout;
+};
+
+struct Program {
+  std::vector<Step> steps;
+  i64 ws_elems = 0;
+};
+
+struct ExecBufs {
+  const float* in_re;
+  const float* in_im;  // NULL for interleaved
+  float* out_re;
+  float* out_im;
+  float2* ws;
+};
+
+struct TwTable {
+  float2* p = nullptr;
+  int S_log2 = 0, H = 0, len = 0;
+};
+
+struct RaderRes {
+  i64 p = 0, g = 0;
+  int* dlog = nullptr;  // dlog[r-1] = log_g r
+  int* src = nullptr;   // src[q] = 1 + perm[(-q) mod (p-1)] = g^-q mod p
+  int* inv = nullptr;   // inverse permutation
+  float2* zs = nullptr; // kernel spectrum / (p-1)
+};
+
+struct ChirpRes {
+  i64 len = 0, pad = 0;
+  float2* chirp = nullptr;  // len entries
+  float2* spec = nullptr;   // pad entries
+};
+
+struct PlanRes {
+  std::vector<void*> allocs;
+  std::map<i64, TwTable> tables;
+  std::map<std::pair<i64, i64>, const float2*> pair_tables;
+  std::map<std::pair<i64, int>, RaderRes> rader;
+  std::map<std::tuple<i64, i64, int>, ChirpRes> chirps;
+  void* dalloc(size_t bytes);
+  TwTable table(i64 n);
+  const float2* pair_table(i64 a, i64 b, int* off_b);
+  const RaderRes& rader_res(i64 p, int sign);
+  const ChirpRes& chirp_res(i64 len, i64 pad, int sign);
+  void release();
+};
+
+bool tile_ok(i64 n);
+cudaError_t run_program(const Program& prog, const ExecBufs& b, cudaStream_t st);
+
+}  // namespace af
+
+struct af_plan_s {
+  long long n = 0;
+  int sign = -1;
+  int algo = 0;
+  af::Planner planner;
+  const af::Node* root = nullptr;
+  af::PlanRes res;
+  std::map<std::pair<long long, int>, af::Program> progs;  // (batch, sign)
+  float2* ws = nullptr;
+  size_t ws_elems = 0;
+  ~af_plan_s();
+};
+
+namespace af {
+void build_program(af_plan_s* P, const Node* root, float sign, i64 batch, Program* prog);
+}

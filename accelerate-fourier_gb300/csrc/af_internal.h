@@ -1,0 +1,63 @@
+// af_internal.h -- declarations shared by libaf's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "af_device.cuh"
+
+namespace af {
+
+// ------------------------------------------------------------- tile kernel
+size_t tile_smem_bytes(const TileDesc& d);
+cudaError_t launch_tile(const TileDesc& d, int threads, cudaStream_t st);
+
+// ------------------------------------------------------------- map kernel
+// Element-wise index maps and pointwise products between two views, one
+// launch over nlines x nout elements.  Integer maps are exact.
+enum MapMode {
+  MAP_COPY = 0,       // out[e] = in[e]
+  MAP_GT_IN = 1,      // out[k*n + j] = in[(n k + m j) mod nm]            (Planned.hs:597-606)
+  MAP_GT_OUT = 2,     // out[r] = in[(r mod n)*m + (r mod m)]            (Planned.hs:608-617)
+  MAP_TABLE = 3,      // out[e] = in[tab[e]]; x0[line] = in[0]           (Permutation.hs:24-33)
+  MAP_RADER_OUT = 4,  // out[0] = x0 + dc; out[r] = x0 + in[tab[r-1]]   (Planned.hs:686-692)
+  MAP_CHIRP_IN = 5,   // out[e] = e < n ? vec[e]*in[e] : 0               (Planned.hs:765-773)
+  MAP_MUL = 6,        // out[e] = vec[e]*in[e]; dc[line] = in[0] if dc
+  MAP_SCALE = 7,      // out[e] = scale*in[e]
+  MAP_REVERSE = 8,    // out[e] = in[(-e) mod n]                         (Cyclic.hs:20-28)
+  MAP_TWIDDLE = 9     // out[e] = in[e] * W_n^((line mod m) * e)         (Planned.hs:555)
+};
+
+struct MapDesc {
+  int mode;
+  i64 nlines, nout;
+  IoDesc in, out;
+  i64 n, m, nm;        // map parameters
+  const int* tab;
+  const float2* vec;
+  float2* dc;          // per-line DC (Rader: sum of the permuted inputs)
+  float2* x0;          // per-line x[0] (Rader)
+  i64 dc_ws, x0_ws;    // workspace offsets of dc / x0 (host side, -1 = none)
+  const float2* tab_tw;  // two-level twiddle table of n (MAP_TWIDDLE)
+  int tw_log2;
+  float tw_sign;
+  float scale;
+};
+cudaError_t launch_map(const MapDesc& d, cudaStream_t st);
+
+// ------------------------------------------------------------- tables (FP64)
+// tab[i] = exp(-2 pi i t_i / n) for the two-level layout: t_i = i (i < S),
+// t_i = (i - S) * S (S <= i < S + H); computed in double, rounded to float.
+cudaError_t launch_twiddle_table(float2* dst, i64 n, int S, int H, cudaStream_t st);
+// chirp[k] = exp(sign * i * pi * sk^2 / len), sk = k for 2k < pad else k - pad,
+// with sk^2 reduced mod 2*len in exact integers (Private.hs:428-436).
+cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cudaStream_t st);
+// Rader kernel[i] = exp(sign * 2 pi i * (g^i mod p) / p) (Planned.hs:655-659)
+cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st);
+
+// ------------------------------------------------------------- other kernels
+cudaError_t launch_karatsuba_i64(const int64_t* x, const int64_t* y, int64_t* z, i64 L, i64 batch,
+                                 int64_t* ws, cudaStream_t st);
+cudaError_t launch_karatsuba_i32(const int32_t* x, const int32_t* y, int64_t* z, i64 L, i64 batch,
+                                 int64_t* ws, cudaStream_t st);
+i64 karatsuba_ws_elems(i64 L, i64 batch);
+
+}  // namespace af

@@ -1,0 +1,143 @@
+// af_kernels.cu -- libaf's element-wise kernels: exact integer index maps
+// (Good-Thomas CRT maps, Rader permutations, cyclic reverse), pointwise
+// spectrum products, and the FP64 generators of twiddle, chirp and Rader
+// kernel tables.
+#include "af_internal.h"
+
+namespace af {
+
+__device__ __forceinline__ i64 view_addr(const IoDesc& io, i64 line, i64 e) {
+  const i64 lo_cnt = io.lo_div.d;
+  const i64 hi = line / lo_cnt;
+  const i64 lo = line - hi * lo_cnt;
+  return hi * io.s_hi + lo * io.s_lo + e * io.s_e;
+}
+__device__ __forceinline__ float2 vload(const IoDesc& io, i64 a) {
+  if (io.c) return io.c[a];
+  return make_float2(io.re[a], io.im[a]);
+}
+__device__ __forceinline__ void vstore(const IoDesc& io, i64 a, float2 v) {
+  if (io.c) io.c[a] = v;
+  else { io.re[a] = v.x; io.im[a] = v.y; }
+}
+
+__global__ void map_kernel(const MapDesc d) {
+  const i64 total = d.nlines * d.nout;
+  for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
+    const i64 line = q / d.nout;
+    const i64 e = q - line * d.nout;
+    float2 v;
+    switch (d.mode) {
+      case MAP_COPY: v = vload(d.in, view_addr(d.in, line, e)); break;
+      case MAP_GT_IN: {
+        const i64 k = e / d.n, j = e - k * d.n;
+        v = vload(d.in, view_addr(d.in, line, (d.n * k + d.m * j) % d.nm));
+        break;
+      }
+      case MAP_GT_OUT:
+        v = vload(d.in, view_addr(d.in, line, (e % d.n) * d.m + (e % d.m)));
+        break;
+      case MAP_TABLE:
+        v = vload(d.in, view_addr(d.in, line, d.tab[e]));
+        if (d.x0 && e == 0) d.x0[line] = vload(d.in, view_addr(d.in, line, 0));
+        break;
+      case MAP_RADER_OUT: {
+        const float2 x0 = d.x0[line];
+        const float2 c = e == 0 ? d.dc[line] : vload(d.in, view_addr(d.in, line, d.tab[e - 1]));
+        v = cadd(x0, c);
+        break;
+      }
+      case MAP_CHIRP_IN:
+        v = e < d.n ? cmul(d.vec[e], vload(d.in, view_addr(d.in, line, e))) : make_float2(0.f, 0.f);
+        break;
+      case MAP_MUL: {
+        const float2 u = vload(d.in, view_addr(d.in, line, e));
+        if (d.dc && e == 0) d.dc[line] = u;
+        v = cmul(d.vec[e], u);
+        break;
+      }
+      case MAP_SCALE: v = cscale(vload(d.in, view_addr(d.in, line, e)), d.scale); break;
+      case MAP_TWIDDLE: {
+        const i64 col = line % d.m;
+        const i64 t = (col * e) % d.n;
+        const float2 lo = d.tab_tw[t & ((1 << d.tw_log2) - 1)];
+        const float2 hi = d.tab_tw[(1 << d.tw_log2) + (t >> d.tw_log2)];
+        float2 w = cmul(hi, lo);
+        w.y *= -d.tw_sign;
+        v = cmul(vload(d.in, view_addr(d.in, line, e)), w);
+        break;
+      }
+      default: {  // MAP_REVERSE
+        const i64 s = e == 0 ? 0 : d.n - e;
+        v = vload(d.in, view_addr(d.in, line, s));
+        break;
+      }
+    }
+    vstore(d.out, view_addr(d.out, line, e), v);
+  }
+}
+
+cudaError_t launch_map(const MapDesc& d, cudaStream_t st) {
+  const i64 total = d.nlines * d.nout;
+  if (total <= 0) return cudaSuccess;
+  i64 blocks = (total + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  map_kernel<<<(unsigned)blocks, 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- FP64 tables
+__global__ void twiddle_table_kernel(float2* dst, i64 n, int S, int H) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S + H) return;
+  i64 t = i < S ? (i64)i : (i64)(i - S) * S;
+  t %= n;
+  double s, c;
+  sincospi(2.0 * (double)t / (double)n, &s, &c);
+  dst[i] = make_float2((float)c, (float)-s);
+}
+cudaError_t launch_twiddle_table(float2* dst, i64 n, int S, int H, cudaStream_t st) {
+  const int tot = S + H;
+  twiddle_table_kernel<<<(tot + 255) / 256, 256, 0, st>>>(dst, n, S, H);
+  return cudaGetLastError();
+}
+
+__global__ void chirp_kernel(double2* dst, i64 pad, i64 len, int sign, i64 count) {
+  const i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const i64 sk = pad > 2 * k ? k : k - pad;
+  const i64 two_len = 2 * len;
+  // pi * sk^2 / len = pi * (sk^2 mod 2 len) / len, exact in integers
+  const unsigned long long r = (unsigned long long)(((__int128)sk * sk) % two_len);
+  double s, c;
+  sincospi((double)r / (double)len, &s, &c);
+  dst[k] = make_double2(c, sign * s);
+}
+cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cudaStream_t st) {
+  chirp_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(dst, pad, len, sign, count);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ i64 mulmod(i64 a, i64 b, i64 m) { return (i64)(((__int128)a * b) % m); }
+
+__global__ void rader_kernel_kernel(double2* dst, i64 p, i64 g, int sign) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p - 1) return;
+  // g^i mod p by square and multiply
+  i64 r = 1, b = g % p, e = i;
+  while (e > 0) {
+    if (e & 1) r = mulmod(r, b, p);
+    b = mulmod(b, b, p);
+    e >>= 1;
+  }
+  double s, c;
+  sincospi(2.0 * (double)r / (double)p, &s, &c);
+  dst[i] = make_double2(c, sign * s);
+}
+cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st) {
+  const i64 cnt = p - 1;
+  rader_kernel_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(dst, p, g, sign);
+  return cudaGetLastError();
+}
+
+}  // namespace af

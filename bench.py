@@ -1,0 +1,344 @@
+"""Benchmark: batched mixed-size C2C FFT, forward + VJP, on one GB300.
+
+Workload (the batched configuration of the reference's headline metric):
+4096 Complex Float32 transforms, lengths n_i = round(exp(U[ln 16, ln 65536]))
+(seed 4); a second seeded draw snaps 50% to the nearest 2^a 3^b 5^c, 25% to
+the next prime >= n_i and leaves 25% raw; data i.i.d. N(0,1) (seed 5);
+spectral weights w ~ U[0,1] (seed 6).  One step = forward transform of every
+signal (the reference's Planned.transform forward), the cotangent
+g = 2 w (.) X of loss sum w|X|^2, and the VJP DFT^H g.  Algorithmic bytes per
+step: 16 N per transform application (read + write), i.e. 32 sum(n_i).
+
+Arms: `--impl ours` (default) runs libaf; `--impl reference` times the CPU
+restatement of the reference algorithm (the oracle; the Haskell reference
+cannot be built here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "accelerate-fourier_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "C2C FFT GB/s & % HBM roofline (fwd+VJP, batched mixed N) vs plain; err vs FP64"
+UNIT = "GB/s"
+COUNT = 4096
+
+
+# ----------------------------------------------------------------- workload
+def smooth235_sorted(limit=1 << 18):
+    vals = []
+    p2 = 1
+    while p2 <= limit:
+        p3 = p2
+        while p3 <= limit:
+            p5 = p3
+            while p5 <= limit:
+                vals.append(p5)
+                p5 *= 5
+            p3 *= 3
+        p2 *= 2
+    return np.array(sorted(vals))
+
+
+def is_prime(n: int) -> bool:
+    if n < 2:
+        return False
+    if n % 2 == 0:
+        return n == 2
+    r = int(math.isqrt(n))
+    for p in range(3, r + 1, 2):
+        if n % p == 0:
+            return False
+    return True
+
+
+def next_prime(n: int) -> int:
+    while not is_prime(n):
+        n += 1
+    return n
+
+
+def workload_sizes(count: int = COUNT, seed: int = 4):
+    rng = np.random.default_rng(seed)
+    base = np.round(np.exp(rng.uniform(math.log(16), math.log(65536), count))).astype(np.int64)
+    cat = rng.uniform(size=count)
+    sm = smooth235_sorted()
+    out = []
+    for n, c in zip(base, cat):
+        n = int(n)
+        if c < 0.5:
+            i = int(np.searchsorted(sm, n))
+            lo = sm[max(i - 1, 0)]
+            hi = sm[min(i, len(sm) - 1)]
+            n = int(lo if (n - lo) <= (hi - n) else hi)
+        elif c < 0.75:
+            n = next_prime(n)
+        out.append(n)
+    return np.array(out, dtype=np.int64)
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- CPU leg
+def cpu_baseline(ns, budget_s: float = 12.0, threads: int = 0):
+    """Oracle (CPU restatement of the reference algorithm) in FP32 on the
+    host cores: forward + inverse-sign transform of a bounded prefix sample of
+    the workload.  Returns (GB/s, cores, sample description)."""
+    from oracle import oracle as O
+    nthreads = threads or O.lib().or_max_threads()
+    fwd = O.Mixed(ns, -1)
+    inv = O.Mixed(ns, +1)
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal(fwd.total) + 1j * rng.standard_normal(fwd.total)).astype(np.complex64)
+    X = np.empty_like(x)
+    G = np.empty_like(x)
+    # grow the prefix until one fwd+inv pass takes ~budget/3, then time it
+    count = 64
+    while True:
+        t0 = time.perf_counter()
+        fwd.exec_f32(x, X, 0, count, nthreads)
+        inv.exec_f32(X, G, 0, count, nthreads)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 3 or count >= len(ns):
+            break
+        count = min(len(ns), int(count * max(2.0, (budget_s / 3) / max(dt, 1e-3))))
+    reps = max(1, int((budget_s * 2 / 3) / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fwd.exec_f32(x, X, 0, count, nthreads)
+        inv.exec_f32(X, G, 0, count, nthreads)
+    dt = (time.perf_counter() - t0) / reps
+    nbytes = 32 * int(ns[:count].sum())
+    sample = f"first {count} of {len(ns)} transforms (sum n = {int(ns[:count].sum())}), fwd + inverse-sign, {reps} reps"
+    return nbytes / dt / 1e9, nthreads, sample
+
+
+# ----------------------------------------------------------------- GPU arm
+class PlainRunner:
+    """One plan per distinct length, one exec per transform (the plain
+    one-launch-per-size path)."""
+
+    def __init__(self, ns):
+        from accelerate_fourier import _lib
+        self.ns = ns
+        self.offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+        self.plans = {}
+        for n in sorted(set(int(v) for v in ns)):
+            self.plans[n] = _lib.Plan(n, -1, "auto")
+        self.launches_per_step = sum(2 * self.plans[int(n)].launches(1) for n in ns)
+
+    def forward(self, x, X, stream):
+        xp, Xp = x.data_ptr(), X.data_ptr()
+        for n, o in zip(self.ns, self.offs):
+            self.plans[int(n)].exec_ptr(xp + 8 * int(o), None, Xp + 8 * int(o), None, 1, stream)
+
+    def vjp(self, g, grad, stream):
+        gp, dp = g.data_ptr(), grad.data_ptr()
+        for n, o in zip(self.ns, self.offs):
+            self.plans[int(n)].exec_ptr(gp + 8 * int(o), None, dp + 8 * int(o), None, 1, stream, vjp=True)
+
+
+def run_ours(args):
+    import torch
+    torch.cuda.set_device(0)
+    ns = workload_sizes()
+    total = int(ns.sum())
+    runner = PlainRunner(ns)
+    rng = np.random.default_rng(5)
+    xh = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    wh = np.random.default_rng(6).uniform(0, 1, total).astype(np.float32)
+    x = torch.from_numpy(xh).cuda()
+    w = torch.from_numpy(wh).cuda()
+    X = torch.empty_like(x)
+    grad = torch.empty_like(x)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        runner.forward(x, X, stream)
+        g = X * (2.0 * w)
+        runner.vjp(g, grad, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+
+    # end to end: pinned host inputs, H2D + step + D2H of the gradient
+    xpin = torch.from_numpy(xh).pin_memory()
+    wpin = torch.from_numpy(wh).pin_memory()
+    gpin = torch.empty_like(xpin).pin_memory()
+
+    def e2e_step():
+        x.copy_(xpin, non_blocking=True)
+        w.copy_(wpin, non_blocking=True)
+        step()
+        gpin.copy_(grad, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+
+    # accuracy vs FP64 oracle on a sample of transforms
+    from oracle import oracle as O
+    step()
+    torch.cuda.synchronize()
+    Xh = X.cpu().numpy()
+    errs = []
+    offs = runner.offs
+    for i in range(0, COUNT, 256):
+        n, o = int(ns[i]), int(offs[i])
+        ref = O.planned(xh[o:o + n].astype(np.complex128)[None], -1)[0]
+        errs.append(np.linalg.norm(Xh[o:o + n] - ref) / np.linalg.norm(ref))
+
+    nbytes = 32 * total
+    value = nbytes / (ms * 1e-3) / 1e9
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    cpu = None
+    if not args.no_cpu:
+        v, cores, sample = cpu_baseline(ns)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
+        "config": {"workload": "4096 mixed-size C2C transforms, n log-uniform [16, 65536] "
+                               "(50% 5-smooth, 25% prime, 25% raw), fwd + VJP",
+                   "sum_n": total, "path": "plain (one plan exec per transform)",
+                   "l2": "inputs (264 MB) larger than L2"},
+        "e2e": {"value": nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+                "h2d_bytes_per_step": int(xh.nbytes + wh.nbytes), "d2h_bytes_per_step": int(xh.nbytes)},
+        "roofline": {"bound": "hbm", "achieved": value, "peak": peak, "unit": "GB/s",
+                     "frac": value / peak, "traffic": None,
+                     "note": "whole-step algorithmic bytes / step time (plain path)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": runner.launches_per_step * args.steps,
+        "clocks": clk,
+        "err_vs_fp64": {"max_rel_l2": float(max(errs)), "median_rel_l2": float(np.median(errs))},
+    }
+    print(json.dumps(out))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    ns = workload_sizes()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(ns, budget_s=3.0)
+    for _ in range(args.steps):
+        v, cores, sample = cpu_baseline(ns, budget_s=6.0)
+        vals.append(v)
+    v = float(np.median(vals))
+    out = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "4096 mixed-size C2C transforms, n log-uniform [16, 65536] "
+                               "(50% 5-smooth, 25% prime, 25% raw), fwd + VJP",
+                   "sum_n": int(ns.sum())},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

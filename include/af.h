@@ -1,0 +1,121 @@
+/*
+ * af.h -- C ABI of libaf, the GB300 (sm_103a) implementation of the
+ * accelerate-fourier transform hot path.
+ *
+ * The reference (accelerate-fourier 1.0.0.5, a Haskell/Accelerate library)
+ * exposes its transforms as Accelerate functions
+ *     type Transform sh a = Acc (Array sh a) -> Acc (Array sh a)
+ * (src/Data/Array/Accelerate/Fourier/Private.hs:29).  A Haskell caller binds
+ * the entry points below with `foreign import ccall` and wraps them in
+ * Accelerate's foreign-function escape hatch; each entry point names the
+ * reference function it replaces.
+ *
+ * Conventions (same as the reference):
+ *   - arrays are row-major; the transform runs over the innermost axis, the
+ *     leading axes are the batch ("sh" in `sh :. Int`);
+ *   - sign -1 is `forward`, +1 is `inverse` (Fourier/Sign.hs:52-54), and no
+ *     transform scales its result (use af_scale_down for Utility.scaleDown);
+ *   - complex data is Complex Float32, either interleaved (re,im pairs) or
+ *     planar (separate re and im arrays, Accelerate's own representation of
+ *     `Array sh (Complex Float)`).
+ * Library conventions:
+ *   - every pointer is a device pointer owned by the caller; every call is
+ *     asynchronous on the given CUDA stream and returns an af_status;
+ *   - the library owns plans, twiddle tables and workspaces (released by
+ *     af_plan_destroy);
+ *   - a plan may be used from one stream at a time;
+ *   - af_last_error() gives a readable message for the calling thread.
+ */
+#ifndef AF_H
+#define AF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* af_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+typedef enum {
+  AF_OK = 0,
+  AF_ERR_INVALID = 1,     /* bad argument (size, sign, pointer, layout)      */
+  AF_ERR_UNSUPPORTED = 2, /* valid request this build cannot run             */
+  AF_ERR_CUDA = 3,        /* a CUDA runtime call failed                      */
+  AF_ERR_ALLOC = 4,       /* device memory could not be allocated            */
+  AF_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up             */
+} af_status;
+
+/* Algorithm selection; each value names the reference function it mirrors. */
+typedef enum {
+  AF_ALGO_AUTO = 0,            /* Planned.transform          (Planned.hs:103-106) */
+  AF_ALGO_DECOMPOSE = 1,       /* Planned.transformDecompose (Planned.hs:114-119) */
+  AF_ALGO_CHIRP2 = 2,          /* Planned.transformChirp2    (Planned.hs:704-708) */
+  AF_ALGO_CHIRP235 = 3,        /* Planned.transformChirp235  (Planned.hs:716-720) */
+  AF_ALGO_PREP_DIT2 = 4,       /* Preprocessed.dit2          (Preprocessed.hs:479-491) */
+  AF_ALGO_PREP_DIF2 = 5,       /* Preprocessed.dif2          (Preprocessed.hs:497-515) */
+  AF_ALGO_PREP_SPLITRADIX = 6, /* Preprocessed.ditSplitRadix (Preprocessed.hs:433-444) */
+  AF_ALGO_ADHOC_AUTO = 7,      /* Adhoc.transform            (Adhoc.hs:74-84)   */
+  AF_ALGO_ADHOC_DIT2 = 8,      /* Adhoc.dit2                 (Adhoc.hs:138-153) */
+  AF_ALGO_ADHOC_SPLITRADIX = 9,/* Adhoc.ditSplitRadix        (Adhoc.hs:101-108) */
+  AF_ALGO_ADHOC_DIT235 = 10,   /* Adhoc.dit235               (Adhoc.hs:171-204) */
+  AF_ALGO_ADHOC_CHIRP2 = 11,   /* Adhoc.transformChirp2      (Adhoc.hs:342-350) */
+  AF_ALGO_ADHOC_CHIRP235 = 12  /* Adhoc.transformChirp235    (Adhoc.hs:355-362) */
+} af_algo;
+
+typedef enum { AF_LAYOUT_INTERLEAVED = 0, AF_LAYOUT_PLANAR = 1 } af_layout;
+
+typedef struct af_plan_s* af_plan;
+
+/* Library identification and the per-thread error message. */
+const char* af_version(void);
+const char* af_last_error(void);
+
+/* Plans -------------------------------------------------------------------
+ * Replaces Planned.plan/cache/transformWithCache (Planned.hs:137-167,201-203,
+ * 322-328): af_plan_create runs the reference planner (bit-exact plan tree) and
+ * builds the device twiddle tables in FP64, rounded to FP32.
+ * Sizes must satisfy 0 <= n; the power-of-two and 5-smooth algorithms need
+ * the sizes the reference functions accept (AF_ERR_INVALID otherwise). */
+af_status af_plan_create(af_plan* plan, int64_t n, int sign, af_algo algo);
+af_status af_plan_destroy(af_plan plan);
+/* The reference plan tree as text, e.g. "GT1001(P13(SR12(SR6(S3))),...)". */
+af_status af_plan_describe(af_plan plan, char* buf, size_t len);
+/* The plan tree of Planned.plan for size n (no device work). */
+af_status af_plan_tree(int64_t n, af_algo algo, char* buf, size_t len);
+/* Number of kernel launches one af_exec_c2c with this batch issues. */
+af_status af_plan_launches(af_plan plan, int64_t batch, int64_t* launches);
+
+/* Complex-to-complex transform over `batch` rows of length n.
+ * Replaces `transform sign len` / `transformWithCache` applied to an array of
+ * shape (batch :. n) (Planned.hs:103-106,137-167) and the Preprocessed/Adhoc
+ * transforms selected at plan time.
+ * INTERLEAVED: in_re/out_re point at float2 data, in_im/out_im are NULL.
+ * PLANAR: separate float arrays.  in == out (in place) is allowed. */
+af_status af_exec_c2c(af_plan plan, af_layout layout, const float* in_re,
+                      const float* in_im, float* out_re, float* out_im,
+                      int64_t batch, af_stream stream);
+
+/* Adjoint (VJP) of af_exec_c2c: grad = DFT^H(cot), i.e. the unscaled transform
+ * of the opposite sign on the cotangent.  The reference has no AD; this is the
+ * gradient of the transform with respect to its input. */
+af_status af_vjp_c2c(af_plan plan, af_layout layout, const float* cot_re,
+                     const float* cot_im, float* grad_re, float* grad_im,
+                     int64_t batch, af_stream stream);
+
+/* Utility.scaleDown (Fourier/Utility.hs:17-26): x *= 1/n over `batch` rows
+ * of length n, in place. */
+af_status af_scale_down(af_layout layout, float* re, float* im, int64_t n,
+                        int64_t batch, af_stream stream);
+
+/* Cyclic.reverse (Cyclic.hs:20-28): out[k] = in[(-k) mod n] per row.
+ * in and out must not overlap. */
+af_status af_cyclic_reverse(af_layout layout, const float* in_re,
+                            const float* in_im, float* out_re, float* out_im,
+                            int64_t n, int64_t batch, af_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,161 @@
+"""GPU parity of the complex-to-complex transforms against the oracle.
+
+Every case runs the CUDA library (through the C ABI) and the oracle (the CPU
+restatement of the reference algorithm, in FP64) on the same seeded input and
+bounds the relative L2 error by c * eps32 * log2 N (eps32 = 2^-24).
+"""
+import numpy as np
+import pytest
+
+from _util import crand, fp32_bound, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _af():
+    from accelerate_fourier import planned, preprocessed, adhoc, utility, cyclic  # noqa: F401
+    import accelerate_fourier as af
+    return af
+
+
+def O():
+    from oracle import oracle
+    return oracle
+
+
+def to_dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x.astype(np.complex64))).cuda()
+
+
+def to_host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy().astype(np.complex128)
+
+
+SMALL = list(range(0, 101))
+MEDIUM = [127, 128, 243, 256, 360, 512, 625, 729, 1000, 1001, 1024, 2048, 2310, 3125, 4096,
+          4097, 6561, 8192, 9973, 10007, 12288, 16384, 16385, 30030]
+LARGE = [65536, 65537, 99991, 1 << 20, 3 ** 12, 1001 * 1024, 1000003]
+
+
+def _check_planned(n, sign, batch, mode, algo, c=3.0, seed=0):
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(seed + n)
+    x = crand(rng, (batch, n))
+    ref = O().planned(x, sign, mode)
+    t = planned.Transform(sign, n, algo)
+    y = to_host(t(to_dev(x)))
+    if n == 0:
+        assert y.shape == x.shape
+        return
+    err = rel_l2(y, ref)
+    bound = fp32_bound(n, c)
+    assert err <= bound, f"n={n} sign={sign} algo={algo} plan={t.describe()} rel_l2={err:.3e} > {bound:.3e}"
+
+
+@pytest.mark.parametrize("n", SMALL)
+def test_planned_small(n):
+    for sign in (-1, 1):
+        _check_planned(n, sign, 3, 0, "auto")
+
+
+@pytest.mark.parametrize("n", MEDIUM)
+def test_planned_medium(n):
+    _check_planned(n, -1, 2, 0, "auto")
+    _check_planned(n, 1, 1, 0, "auto")
+
+
+@pytest.mark.parametrize("n", LARGE)
+def test_planned_large(n):
+    _check_planned(n, -1, 1, 0, "auto", c=4.0)
+
+
+@pytest.mark.parametrize("n", [2, 3, 7, 10, 17, 100, 101, 1000, 4099])
+@pytest.mark.parametrize("mode,algo", [(1, "decompose"), (2, "chirp2"), (3, "chirp235")])
+def test_planned_algorithms(n, mode, algo):
+    _check_planned(n, -1, 2, mode, algo, c=6.0)
+
+
+VARIANTS = [("prep_dit2", 0, "pow2"), ("prep_dif2", 1, "pow2"), ("prep_splitradix", 2, "pow2"),
+            ("adhoc_dit2", 3, "pow2"), ("adhoc_splitradix", 4, "pow2"), ("adhoc_dit235", 5, "smooth"),
+            ("adhoc_chirp2", 6, "any"), ("adhoc_chirp235", 7, "any"), ("adhoc_auto", 8, "any")]
+
+
+@pytest.mark.parametrize("algo,code,kind", VARIANTS)
+def test_variants(algo, code, kind):
+    from accelerate_fourier import planned
+    sizes = {"pow2": [1, 2, 4, 8, 64, 1024, 4096],
+             "smooth": [1, 2, 3, 5, 6, 9, 15, 30, 360, 1000, 3375],
+             "any": [1, 2, 3, 7, 11, 30, 97, 100, 1009]}[kind]
+    rng = np.random.default_rng(code)
+    for n in sizes:
+        for sign in (-1, 1):
+            x = crand(rng, (2, n))
+            ref = O().variant(x, sign, code)
+            y = to_host(planned.Transform(sign, n, algo)(to_dev(x)))
+            assert rel_l2(y, ref) <= fp32_bound(n, 6.0), (algo, n, sign)
+
+
+def test_round_trip_config1():
+    """N=1024, batch 64, U[-1,1]: forward, inverse, scaleDown gives x back."""
+    from accelerate_fourier import planned, utility
+    rng = np.random.default_rng(1)
+    x = crand(rng, (64, 1024))
+    xd = to_dev(x)
+    X = planned.transform(-1, 1024)(xd)
+    back = to_host(utility.scaleDown(planned.transform(1, 1024)(X)))
+    assert rel_l2(back, x) <= fp32_bound(1024, 3.0)
+    ref = O().planned(x, -1)
+    assert rel_l2(to_host(X), ref) <= fp32_bound(1024, 3.0)
+
+
+@pytest.mark.parametrize("n", [8, 13, 100, 1001, 4096, 65537])
+def test_vjp_is_adjoint(n):
+    """<F x, y> = <x, F^H y> with F^H the library's VJP."""
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(n)
+    x = crand(rng, (2, n))
+    g = crand(rng, (2, n))
+    t = planned.transform(-1, n)
+    fx = to_host(t(to_dev(x)))
+    vg = to_host(t.vjp(to_dev(g)))
+    lhs = np.vdot(g, fx)
+    rhs = np.vdot(vg, x)
+    assert abs(lhs - rhs) <= 1e-5 * (abs(lhs) + np.linalg.norm(x) * np.linalg.norm(g) * np.sqrt(n))
+    ref = O().planned(g, +1)
+    assert rel_l2(vg, ref) <= fp32_bound(n, 4.0)
+
+
+@pytest.mark.parametrize("n", [16, 1000, 4096, 65537])
+def test_planar_layout(n):
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(7)
+    x = crand(rng, (3, n))
+    re = torch.from_numpy(x.real.astype(np.float32)).cuda()
+    im = torch.from_numpy(x.imag.astype(np.float32)).cuda()
+    ore, oim = planned.transform(-1, n)((re, im))
+    torch.cuda.synchronize()
+    y = ore.cpu().numpy() + 1j * oim.cpu().numpy()
+    assert rel_l2(y, O().planned(x, -1)) <= fp32_bound(n, 3.0)
+
+
+@pytest.mark.parametrize("n", [64, 1001, 65537, 1 << 20])
+def test_in_place(n):
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(9)
+    x = crand(rng, (1, n))
+    d = to_dev(x)
+    planned.transform(-1, n)(d, out=d)
+    assert rel_l2(to_host(d), O().planned(x, -1)) <= fp32_bound(n, 4.0)
+
+
+def test_cyclic_reverse_and_scale_exact():
+    from accelerate_fourier import cyclic, utility
+    rng = np.random.default_rng(3)
+    x = crand(rng, (4, 37)).astype(np.complex64)
+    y = to_host(cyclic.reverse(to_dev(x)))
+    assert np.array_equal(y, O().cyclic_reverse(x.astype(np.complex128)).astype(np.complex64))
+    s = to_host(utility.scaleDown(to_dev(x)))
+    assert np.allclose(s, x / 37, rtol=1e-6, atol=0)
