@@ -1031,23 +1031,24 @@ void or_convolve_cyclic(i64 n, i64 batch, const double* x, const double* yv, dou
   or_handle_destroy(f);
 }
 
-// Convolution/Adhoc.hs:36-98 karatsuba (loop form) over int64 rows of length L;
-// output rows of length max 0 (2L-1).
-void or_karatsuba_loop_i64(i64 L, i64 batch, const i64* x, const i64* y, i64* z) {
+// Convolution/Adhoc.hs:36-98 karatsuba (loop form) over rows of length L;
+// output rows of length max 0 (2L-1).  Generic over the ring (int64, double).
+}  // extern "C"
+template <class R>
+static void karatsuba_loop(i64 L, i64 batch, const R* x, const R* y, R* z) {
   i64 zl = L > 0 ? 2 * L - 1 : 0;
   for (i64 b = 0; b < batch; ++b) {
-    // state rows (count x len)
-    std::vector<i64> xs(x + b * L, x + (b + 1) * L), ys(y + b * L, y + (b + 1) * L);
+    std::vector<R> xs(x + b * L, x + (b + 1) * L), ys(y + b * L, y + (b + 1) * L);
     i64 cnt = 1, len = L;
     std::vector<i64> lens = {L};
     while (len > 1) {  // karatsubaReorder (Adhoc.hs:66-79)
       i64 l2 = (len + 1) / 2;
-      std::vector<i64> nx(3 * cnt * l2), ny(3 * cnt * l2);
+      std::vector<R> nx(3 * cnt * l2), ny(3 * cnt * l2);
       for (i64 r = 0; r < cnt; ++r)
         for (i64 j = 0; j < l2; ++j) {
-          i64 xl = xs[r * len + j], yl = ys[r * len + j];
-          i64 xr = (l2 + j < len) ? xs[r * len + l2 + j] : 0;
-          i64 yr = (l2 + j < len) ? ys[r * len + l2 + j] : 0;
+          R xl = xs[r * len + j], yl = ys[r * len + j];
+          R xr = (l2 + j < len) ? xs[r * len + l2 + j] : R(0);
+          R yr = (l2 + j < len) ? ys[r * len + l2 + j] : R(0);
           nx[r * l2 + j] = xl; nx[(cnt + r) * l2 + j] = xl + xr; nx[(2 * cnt + r) * l2 + j] = xr;
           ny[r * l2 + j] = yl; ny[(cnt + r) * l2 + j] = yl + yr; ny[(2 * cnt + r) * l2 + j] = yr;
         }
@@ -1055,28 +1056,35 @@ void or_karatsuba_loop_i64(i64 L, i64 batch, const i64* x, const i64* y, i64* z)
       cnt *= 3; len = l2;
       lens.insert(lens.begin(), len);
     }
-    std::vector<i64> zz(cnt * len);
+    std::vector<R> zz(cnt * len);
     for (i64 i = 0; i < cnt * len; ++i) zz[i] = xs[i] * ys[i];
-    i64 zlen_cur = len;  // current row length of zz
-    while (lens.size() > 1) {  // karatsubaGo (Adhoc.hs:81-98)
+    i64 zlen_cur = len;
+    while (lens.size() > 1) {  // karatsubaGo (Adhoc.hs:81-98), indexPad (Convolution/Private.hs:21-26)
       i64 xlen = lens[0], zlen = 2 * lens[1] - 1;
       i64 n3 = cnt / 3;
-      std::vector<i64> nz(n3 * zlen, 0);
-      auto at = [&](i64 row, i64 k) -> i64 { return (k >= 0 && k < zlen_cur) ? zz[row * zlen_cur + k] : 0; };
+      std::vector<R> nz(n3 * zlen, R(0));
+      auto at = [&](i64 row, i64 k) -> R { return (k >= 0 && k < zlen_cur) ? zz[row * zlen_cur + k] : R(0); };
       for (i64 r = 0; r < n3; ++r)
         for (i64 k = 0; k < zlen; ++k) {
-          i64 lv = at(r, k);
+          R lv = at(r, k);
           i64 kc = k - xlen, kr = k - 2 * xlen;
-          i64 cv = (kc >= 0 && kc < zlen_cur) ? at(n3 + r, kc) - (at(r, kc) + at(2 * n3 + r, kc)) : 0;
-          i64 rv = at(2 * n3 + r, kr);
+          R cv = (kc >= 0 && kc < zlen_cur) ? at(n3 + r, kc) - (at(r, kc) + at(2 * n3 + r, kc)) : R(0);
+          R rv = at(2 * n3 + r, kr);
           nz[r * zlen + k] = lv + cv + rv;
         }
       zz.swap(nz);
       cnt = n3; zlen_cur = zlen;
       lens.erase(lens.begin());
     }
-    for (i64 k = 0; k < zl; ++k) z[b * zl + k] = (k < zlen_cur) ? zz[k] : 0;
+    for (i64 k = 0; k < zl; ++k) z[b * zl + k] = (k < zlen_cur) ? zz[k] : R(0);
   }
+}
+extern "C" {
+void or_karatsuba_loop_i64(i64 L, i64 batch, const i64* x, const i64* y, i64* z) {
+  karatsuba_loop<i64>(L, batch, x, y, z);
+}
+void or_karatsuba_loop_f64(i64 L, i64 batch, const double* x, const double* y, double* z) {
+  karatsuba_loop<double>(L, batch, x, y, z);
 }
 
 // Convolution/Preprocessed.hs:29-56 karatsuba (recursive form), int64

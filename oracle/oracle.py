@@ -78,6 +78,7 @@ def lib():
             "or_convolve_cyclic": ([I64, I64, PTR, PTR, PTR], None),
             "or_karatsuba_loop_i64": ([I64, I64, PTR, PTR, PTR], None),
             "or_karatsuba_rec_i64": ([I64, I64, PTR, PTR, PTR], None),
+            "or_karatsuba_loop_f64": ([I64, I64, PTR, PTR, PTR], None),
             "or_cyclic_fold_i64": ([I64, I64, PTR, PTR], None),
             "or_mixed_create": ([ctypes.c_int, ctypes.c_int, I64, PTR], PTR),
             "or_mixed_destroy": ([PTR], None),
@@ -263,6 +264,39 @@ def karatsuba(x, y, recursive: bool = False) -> np.ndarray:
         f = lib().or_karatsuba_rec_i64 if recursive else lib().or_karatsuba_loop_i64
         f(L, batch, _p(x), _p(y), _p(out))
     return out
+
+
+def karatsuba_f64(x, y) -> np.ndarray:
+    """Convolution.Adhoc.karatsuba over Double rows (loop form)."""
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    y = np.ascontiguousarray(np.asarray(y, dtype=np.float64))
+    L, batch = _rows(x)
+    out = np.zeros(x.shape[:-1] + (max(0, 2 * L - 1),), dtype=np.float64)
+    if x.size:
+        lib().or_karatsuba_loop_f64(L, batch, _p(x), _p(y), _p(out))
+    return out
+
+
+def karatsuba_complex(x, y, cyclic: bool = False) -> np.ndarray:
+    """Convolution.Adhoc.complex (3 real products, Convolution/Adhoc.hs:118-133)
+    of karatsuba, optionally through Convolution.Adhoc.cyclic (104-111)."""
+    x = _c128(x)
+    y = _c128(y)
+    xr, xi, yr, yi = x.real.copy(), x.imag.copy(), y.real.copy(), y.imag.copy()
+    xm, ym = xr + xi, yr + yi
+
+    def conv(a, b):
+        z = karatsuba_f64(a, b)
+        if cyclic:
+            L = a.shape[-1]
+            if L == 0:
+                return z
+            w = z[..., :L].copy()
+            w[..., :L - 1] += z[..., L:]
+            return w
+        return z
+    rr, ii, mm = conv(xr, yr), conv(xi, yi), conv(xm, ym)
+    return (rr - ii) + 1j * (mm - (rr + ii))
 
 
 def cyclic_fold(z, L: int) -> np.ndarray:
