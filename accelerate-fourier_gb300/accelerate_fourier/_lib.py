@@ -41,6 +41,12 @@ SIGNATURES = {
     "af_vjp_c2c": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_scale_down": ([INT, PTR, PTR, I64, I64, PTR], INT),
     "af_cyclic_reverse": ([INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_batch_create": ([ctypes.POINTER(PTR), PTR, I64, INT], INT),
+    "af_batch_destroy": ([PTR], INT),
+    "af_batch_launches": ([PTR, ctypes.POINTER(I64)], INT),
+    "af_batch_exec": ([PTR, PTR, PTR, PTR], INT),
+    "af_batch_vjp": ([PTR, PTR, PTR, PTR], INT),
+    "af_batch_forward_cotangent": ([PTR, PTR, PTR, PTR, PTR, PTR], INT),
 }
 
 
@@ -122,6 +128,41 @@ class Plan:
         try:
             if self._h:
                 load().af_plan_destroy(self._h)
+                self._h = PTR()
+        except Exception:
+            pass
+
+
+class Batch:
+    """An af_batch: many transforms of mixed lengths stored back to back."""
+
+    def __init__(self, lengths, sign: int = -1):
+        import numpy as np
+        self.lengths = np.ascontiguousarray(np.asarray(lengths, dtype=np.int64))
+        self.sign = int(sign)
+        self.total = int(self.lengths.sum())
+        self._h = PTR()
+        check(load().af_batch_create(ctypes.byref(self._h), self.lengths.ctypes.data, len(self.lengths),
+                                     self.sign))
+
+    def launches(self) -> int:
+        out = I64()
+        check(load().af_batch_launches(self._h, ctypes.byref(out)))
+        return out.value
+
+    def exec_ptr(self, src, dst, stream=0):
+        check(load().af_batch_exec(self._h, src, dst, stream))
+
+    def vjp_ptr(self, src, dst, stream=0):
+        check(load().af_batch_vjp(self._h, src, dst, stream))
+
+    def forward_cotangent_ptr(self, x, w, cot, loss, stream=0):
+        check(load().af_batch_forward_cotangent(self._h, x, w, cot, loss, stream))
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().af_batch_destroy(self._h)
                 self._h = PTR()
         except Exception:
             pass

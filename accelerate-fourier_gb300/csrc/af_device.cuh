@@ -64,55 +64,94 @@ struct FftPhase {
   PassDesc pass[AF_MAXP];
 };
 
+// Buffers a launch addresses: every IoDesc names one of them and the launch
+// passes their base pointers (interleaved `c`, or planar `re`/`im` planes).
+enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_AUX = 3, BUF_COUNT = 4 };
+struct TileBases {
+  float2* c[BUF_COUNT];
+  float* re[BUF_COUNT];
+  float* im[BUF_COUNT];
+};
+
+// Index maps of one side of a tile (element e of a line with lo index `lo`).
+enum IoMap {
+  IO_AFFINE = 0,  // hi*s_hi + lo*s_lo + e*s_e
+  IO_GT = 1,      // hi*s_hi + ((mA*lo + mB*e) mod mN)*s_t   Good-Thomas CRT map
+  IO_TABLE = 2,   // hi*s_hi + tab[q]*s_t, q = lo*q_lo + e*q_e (Rader gather)
+  IO_CHIRP = 3,   // q < mN ? vec[q] * x[hi*s_hi + q*s_t] : 0 (load); vec[q]*v (store, q < mN)
+  IO_RADER = 4    // store: out[tab[q]] = x0 + v; q == 0 also writes out[0] = x0 + dc
+};
+
 // Global-memory view of one side (input or output) of a tile program.
-// A tile "line" l of a launch is split as hi = l / lo_count, lo = l % lo_count,
-// and element e of that line lives at  hi*s_hi + lo*s_lo + e*s_e  (complex
-// units).  Planar layout uses re/im float planes with the same indexing.
+// A tile "line" l of a launch is split as hi = l / lo_count, lo = l % lo_count.
 struct IoDesc {
-  float2* c;        // interleaved base, or NULL
-  float* re;        // planar re plane (when c == NULL)
-  float* im;        // planar im plane
+  int buf;
+  int map;
+  int line_fast;    // 1: consecutive threads walk lines (strided element access)
+  int x0_buf;       // IO_RADER: buffer holding the transform inputs (x0 = x[hi][0])
+  i64 off;          // complex-unit offset into the buffer
   i64 s_e, s_lo, s_hi;
   FastDiv lo_div;
-  int line_fast;    // 1: consecutive threads walk lines (strided element access)
+  i64 q_lo, q_e;    // logical index q = lo*q_lo + e*q_e
+  i64 mA, mB, mN;   // GT map constants / logical length for IO_CHIRP
+  i64 s_t;          // element stride of a mapped transform
+  const int* tab;
+  const float2* vec;
+  i64 x0_off, x0_shi;  // IO_RADER: x0 at x0_off + hi*x0_shi in buffer x0_buf
+  i64 dc_off;          // IO_RADER: DC of transform hi at ws[dc_off + hi]
 };
 
 enum TileKind {
-  TILE_PLAIN = 0,     // load -> FFT -> store
+  TILE_PLAIN = 0,     // load -> FFT -> store (with the IoDesc maps)
   TILE_GT = 1,        // Good-Thomas: CRT load -> FFT_n rows -> FFT_m cols -> CRT store
   TILE_RADER = 2,     // Rader: dlog gather -> FFT(+1) -> *zs -> FFT(-1) -> dlog scatter + x0
-  TILE_BLUESTEIN = 3  // Bluestein: chirp*x, pad -> FFT(+1) -> *spec -> FFT(-1) -> chirp*, take N
+  TILE_BLUESTEIN = 3, // Bluestein: chirp*x, pad -> FFT(+1) -> *spec -> FFT(-1) -> chirp*, take N
+  TILE_CONVROW = 4    // four-step conv middle: row FFT(+1) -> *S[q] -> row FFT(-1) -> twiddle
 };
 
 struct TileDesc {
   int kind;
   int nlen;          // logical transform length N seen through in/out
-  int G;             // transforms ("lines" of the launch) per CTA
-  int nlines;        // total lines of the launch
-  int LS;            // shared-memory stride between transforms (unpadded units)
-  int slen;          // elements per transform held in shared memory (M for conv tiles)
+  int G;             // lines per full CTA
+  int nlines;        // total lines of the step (all CTAs)
+  int LS;            // shared-memory stride between lines (unpadded units)
+  int slen;          // elements per line held in shared memory (M for conv tiles)
   int tw_total;      // float2 table entries staged in shared memory
+  int nph;
   const float2* tw_src;  // table source (device)
   FftPhase ph[AF_MAXPH];
-  int nph;
   FastDiv N_div, S_div, G_div;  // nlen, slen, G
   IoDesc in, out;
   float scale;       // multiplies every stored element
-  // four-step post twiddle: element e of a line with column c = lo*ptw_col_mul
-  // is multiplied by W_N^(c*e) (two-level table: S lo entries then hi entries)
+  float ptw_sign;
+  // four-step twiddle on store: element e of a line with lo index c is
+  // multiplied by W_N^(c*e) (two-level table: S lo entries then hi entries)
   const float2* ptw;
   int ptwS_log2;
+  int cot;           // 1: store g = 2 w v (w read from BUF_AUX at the output
+                     // address) and add w |v|^2 to the loss
   i64 ptwN;
-  int ptw_col_mul;
-  float ptw_sign;
-  // Good-Thomas grid m x n: logical input i sits at ((i*gt_cm) mod m)*n + (i*gt_cn) mod n
+  // Good-Thomas tile grid m x n: logical input i sits at ((i*cm) mod m)*n + (i*cn) mod n
   int gt_n, gt_m;
   i64 gt_cm, gt_cn;
   // Rader: dlog[r-1] = log_g(r) for r = 1..p-1
   const int* dlog;
-  // Bluestein chirp (N entries); conv spectrum (slen entries): Rader zs / chirp spectrum
+  // Bluestein chirp (N entries); conv spectrum (Rader zs / chirp spectrum / S)
   const float2* vec_a;
   const float2* vec_b;
+  // TILE_CONVROW: spectrum index q = lo*sq_lo + e*sq_e; DC of line lo == 0,
+  // element 0 after the first FFT goes to ws[dc_off + hi] (dc_off < 0: none)
+  i64 sq_lo, sq_e, dc_off;
+};
+
+// One CTA's work in a launch: lines [line0, line0 + G) of descriptor `desc`;
+// the *_add offsets shift the in/out/aux views (per-transform placement).
+struct WorkItem {
+  int desc;
+  int line0;
+  int G;
+  int pad;
+  i64 in_add, out_add, aux_add;
 };
 
 // ---------------------------------------------------------------- smem layout

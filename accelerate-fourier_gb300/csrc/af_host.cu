@@ -124,10 +124,23 @@ static std::vector<float2> to_f32(const std::vector<cd>& v) {
   return o;
 }
 
+// Length of the transforms carrying a Rader convolution of length p-1:
+// p-1 itself when it is 13-smooth (the reference's Rader), otherwise the
+// least 13-smooth M >= 2(p-1)-1, so that the cyclic convolution of length p-1
+// runs as one zero-padded convolution instead of nested Rader transforms.
+i64 rader_conv_len(i64 p) {
+  const i64 m = p - 1;
+  if (is_13smooth(m)) return m;
+  i64 M = 2 * m - 1;
+  while (!is_13smooth(M)) ++M;
+  return M;
+}
+
 // Planned.hs:650-664 levelCachePrime: permutations and the kernel spectrum
 // zs = scaleDown (inverse-direction transform of kernel), kernel[i] = W^(g^i).
 const RaderRes& PlanRes::rader_res(i64 p, int sign) {
   auto key = std::make_pair(p, sign);
+  const i64 M = rader_conv_len(p);
   auto it = rader.find(key);
   if (it != rader.end()) return it->second;
   RaderRes r;
@@ -142,27 +155,39 @@ const RaderRes& PlanRes::rader_res(i64 p, int sign) {
     dlog[x - 1] = (int)i;
     x = (i64)((__int128)x * r.g % p);
   }
+  std::vector<int> gpow(m);
   for (i64 q = 0; q < m; ++q) src[q] = (int)(1 + perm[(m - q) % m]);  // 1 + reverse perm (75-80)
   for (i64 k = 0; k < m; ++k) inv[k] = dlog[k];                       // inverse perm (68-73)
+  for (i64 q = 0; q < m; ++q) gpow[q] = (int)(1 + perm[q]);
   r.dlog = (int*)dalloc(sizeof(int) * m);
   r.src = (int*)dalloc(sizeof(int) * m);
   r.inv = (int*)dalloc(sizeof(int) * m);
+  r.gpow = (int*)dalloc(sizeof(int) * m);
   cuda_check(cudaMemcpy(r.dlog, dlog.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.src, src.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.inv, inv.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
+  cuda_check(cudaMemcpy(r.gpow, gpow.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   // kernel in FP64 on the device, spectrum in FP64 on the host
   double2* dk = nullptr;
   cuda_check(cudaMalloc(&dk, sizeof(double2) * m), "rader kernel");
   cudaError_t e = launch_rader_kernel(dk, p, r.g, sign, 0);
-  std::vector<cd> kern(m), spec(m);
+  std::vector<cd> kern(m);
   if (e == cudaSuccess) e = cudaMemcpy(kern.data(), dk, sizeof(double2) * m, cudaMemcpyDeviceToHost);
   cudaFree(dk);
   cuda_check(e, "rader kernel");
-  fft64(kern.data(), 1, spec.data(), m, +1);
-  for (auto& v : spec) v /= (double)m;
-  std::vector<float2> zs = to_f32(spec);
-  r.zs = (float2*)dalloc(sizeof(float2) * m);
-  cuda_check(cudaMemcpy(r.zs, zs.data(), sizeof(float2) * m, cudaMemcpyHostToDevice), "rader spectrum");
+  // cyclic convolution of length m computed with transforms of length M >= m:
+  // the kernel is placed periodically, kk[i] = k[i], kk[M-i] = k[m-i] (0 < i < m);
+  // for M = m this is the reference's kernel spectrum
+  std::vector<cd> kk(M, cd(0, 0)), S(M);
+  for (i64 i = 0; i < m; ++i) kk[i] = kern[i];
+  if (M > m)
+    for (i64 i = 1; i < m; ++i) kk[M - i] = kern[m - i];
+  fft64(kk.data(), 1, S.data(), M, +1);
+  for (auto& v : S) v /= (double)M;
+  std::vector<float2> zs = to_f32(S);
+  r.zs = (float2*)dalloc(sizeof(float2) * M);
+  r.M = M;
+  cuda_check(cudaMemcpy(r.zs, zs.data(), sizeof(float2) * M, cudaMemcpyHostToDevice), "rader spectrum");
   rader[key] = r;
   return rader[key];
 }
@@ -196,6 +221,7 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
   return chirps[key];
 }
 
+
 // ============================================================ tile building
 // elements per CTA the ping-pong tile can hold (two padded buffers + tables)
 static const i64 kTileCap = 13000;
@@ -214,6 +240,25 @@ static std::vector<int> radices(i64 n) {
 }
 
 bool tile_ok(i64 n) { return n >= 1 && n <= kTileCap && is_13smooth(n); }
+
+// (n1, n2) with n = n1 n2, both tile lengths, n1 (the strided column
+// transform) near sqrt(n) and at most 1024; false if no such split exists
+static bool four_step_split(i64 n, i64* n1, i64* n2) {
+  if (!is_13smooth(n)) return false;
+  i64 best = 0;
+  double bestd = 1e30;
+  for (i64 a = 2; a <= 1024 && a * a <= n * 4; ++a) {
+    if (n % a) continue;
+    const i64 b = n / a;
+    if (!tile_ok(a) || !tile_ok(b)) continue;
+    const double d = std::fabs(std::log((double)a) - 0.5 * std::log((double)n));
+    if (d < bestd) { bestd = d; best = a; }
+  }
+  if (!best) return false;
+  *n1 = best;
+  *n2 = n / best;
+  return true;
+}
 
 static void fill_phase(FftPhase& ph, i64 n, float sign, int ls, int es, int lcnt, int tw_off, int S_log2) {
   memset(&ph, 0, sizeof ph);
@@ -243,20 +288,25 @@ static void fill_phase(FftPhase& ph, i64 n, float sign, int ls, int es, int lcnt
 static IoDesc io_of(const View& v) {
   IoDesc io;
   memset(&io, 0, sizeof io);
+  io.buf = v.buf;
+  io.map = IO_AFFINE;
+  io.off = v.off;
   io.s_e = v.s_e;
   io.s_lo = v.s_lo;
   io.s_hi = v.s_hi;
+  io.s_t = 1;
   io.lo_div = make_fastdiv((unsigned)std::min<i64>(v.lo_cnt, (i64)1 << 30));
   io.line_fast = v.s_e != 1 && v.s_lo == 1;
+  io.dc_off = -1;
   return io;
 }
 
-// choose threads per CTA and lines per CTA (G) for a tile whose shared
-// footprint per line is `slen` elements; want_wide asks for >= 16 lines so
-// that strided (line-fast) global access moves whole sectors
+// threads per CTA and lines per CTA (G) for a tile with `slen` shared
+// elements per line; want_wide asks for >= 16 lines so that strided
+// (line-fast) global access moves whole 32-byte sectors
 static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, int* threads, int* G) {
-  const i64 budget = 227 * 1024 - (i64)sizeof(FftPhase) * AF_MAXPH - 8 * (i64)tw_total - 256;
-  auto fits = [&](i64 g) { return 2 * 8 * (g * slen + ((g * slen) >> 4)) + 16 * g <= budget; };
+  const i64 budget = 227 * 1024 - (i64)sizeof(TileDesc) - 8 * (i64)tw_total - 512;
+  auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) + 16 * g <= budget; };
   i64 g = std::max<i64>(1, 4096 / std::max<i64>(slen, 1));
   if (want_wide) g = std::max<i64>(g, 16);
   g = std::min(g, std::max<i64>(lines, 1));
@@ -267,9 +317,464 @@ static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, i
   *threads = elems >= 6144 ? 512 : (elems >= 1024 ? 256 : 128);
 }
 
-// ============================================================ lowering
+struct TileStep {
+  TileDesc d;
+  int threads = 128;
+  i64 lines = 0;
+};
+
+static void finish_geometry(TileStep& s, i64 slen, bool want_wide) {
+  int threads, G;
+  choose_geometry(slen, s.lines, s.d.tw_total, want_wide, &threads, &G);
+  s.threads = threads;
+  s.d.G = G;
+  s.d.nlines = (int)s.lines;
+  s.d.G_div = make_fastdiv((unsigned)G);
+  s.d.N_div = make_fastdiv((unsigned)s.d.nlen);
+  s.d.S_div = make_fastdiv((unsigned)s.d.slen);
+}
+
+static TileDesc blank_desc() {
+  TileDesc d;
+  memset(&d, 0, sizeof d);
+  d.scale = 1.f;
+  d.dc_off = -1;
+  return d;
+}
+
+// plain tile: FFT of length n (sign) over `lines` lines, optional store twiddle W_ptwN^(lo e)
+static TileStep plain_step(PlanRes& res, i64 n, float sign, i64 lines, const View& in, const View& out,
+                           i64 ptwN = 0) {
+  TileStep s;
+  s.d = blank_desc();
+  TileDesc& d = s.d;
+  d.kind = TILE_PLAIN;
+  d.nlen = (int)n;
+  d.slen = (int)n;
+  d.LS = (int)n;
+  TwTable t = res.table(n);
+  d.tw_src = t.p;
+  d.tw_total = t.len;
+  fill_phase(d.ph[0], n, sign, (int)n, 1, 1, 0, t.S_log2);
+  d.nph = 1;
+  d.in = io_of(in);
+  d.out = io_of(out);
+  if (ptwN) {
+    TwTable pt = res.table(ptwN);
+    d.ptw = pt.p;
+    d.ptwS_log2 = pt.S_log2;
+    d.ptwN = ptwN;
+    d.ptw_sign = sign;
+  }
+  s.lines = lines;
+  finish_geometry(s, n, d.in.line_fast || d.out.line_fast);
+  return s;
+}
+
+static i64 mod_inverse(i64 a, i64 m) {
+  if (m == 1) return 0;
+  i64 t = 0, nt = 1, r = m, nr = ((a % m) + m) % m;
+  while (nr) {
+    const i64 q = r / nr;
+    i64 tmp = t - q * nt; t = nt; nt = tmp;
+    tmp = r - q * nr; r = nr; nr = tmp;
+  }
+  return t < 0 ? t + m : t;
+}
+
+static bool gt_tile_ok(const Node* nd) {
+  return nd->kind == N_COPRIME && nd->n <= kTileCap && tile_ok(nd->a->n) && tile_ok(nd->b->n);
+}
+static bool rader_tile_ok(const Node* nd) {
+  return nd->kind == N_PRIME && nd->n > 13 && tile_ok(rader_conv_len(nd->n));
+}
+static bool chirp_tile_ok(const Node* nd) { return nd->kind == N_CHIRP && tile_ok(nd->a->n); }
+static bool plain_ok(const Node* nd) {
+  return tile_ok(nd->n) && nd->kind != N_CHIRP && !(nd->kind == N_PRIME && nd->n > 13);
+}
+static bool single_tile_ok(const Node* nd) {
+  return nd->n <= 1 || gt_tile_ok(nd) || rader_tile_ok(nd) || chirp_tile_ok(nd) || plain_ok(nd);
+}
+
+// Good-Thomas tile (Planned.hs:584-617): grid m x n, n = first factor
+static TileStep gt_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
+  TileStep s;
+  s.d = blank_desc();
+  TileDesc& d = s.d;
+  d.kind = TILE_GT;
+  d.nlen = (int)N;
+  d.slen = (int)N;
+  d.LS = (int)N;
+  int offb = 0;
+  d.tw_src = res.pair_table(n, m, &offb);
+  d.tw_total = res.table(n).len + res.table(m).len;
+  fill_phase(d.ph[0], n, sign, (int)n, 1, (int)m, 0, res.table(n).S_log2);     // rows (j)
+  fill_phase(d.ph[1], m, sign, 1, (int)n, (int)n, offb, res.table(m).S_log2);  // cols (k)
+  d.nph = 2;
+  d.gt_n = (int)n;
+  d.gt_m = (int)m;
+  d.gt_cm = mod_inverse(n, m);  // i = (n k + m j) mod N  =>  k = i n^-1 mod m
+  d.gt_cn = mod_inverse(m, n);  //                           j = i m^-1 mod n
+  d.in = io_of(in);
+  d.out = io_of(out);
+  d.in.line_fast = d.out.line_fast = 0;
+  s.lines = lines;
+  finish_geometry(s, N, false);
+  return s;
+}
+
+// Rader tile (Planned.hs:646-692), convolution length M = rader_conv_len(p)
+static TileStep rader_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  const i64 p = nd->n;
+  const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
+  const i64 M = rr.M;
+  TileStep s;
+  s.d = blank_desc();
+  TileDesc& d = s.d;
+  d.kind = TILE_RADER;
+  d.nlen = (int)p;
+  d.slen = (int)M;
+  d.LS = (int)M;
+  TwTable t = res.table(M);
+  d.tw_src = t.p;
+  d.tw_total = t.len;
+  fill_phase(d.ph[0], M, +1.f, (int)M, 1, 1, 0, t.S_log2);
+  fill_phase(d.ph[1], M, -1.f, (int)M, 1, 1, 0, t.S_log2);
+  d.nph = 2;
+  d.dlog = rr.dlog;
+  d.vec_b = rr.zs;
+  d.in = io_of(in);
+  d.out = io_of(out);
+  d.in.line_fast = d.out.line_fast = 0;
+  s.lines = lines;
+  finish_geometry(s, M, false);
+  return s;
+}
+
+// Bluestein tile (Planned.hs:760-773)
+static TileStep chirp_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  const i64 N = nd->n, M = nd->a->n;
+  const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
+  TileStep s;
+  s.d = blank_desc();
+  TileDesc& d = s.d;
+  d.kind = TILE_BLUESTEIN;
+  d.nlen = (int)N;
+  d.slen = (int)M;
+  d.LS = (int)M;
+  TwTable t = res.table(M);
+  d.tw_src = t.p;
+  d.tw_total = t.len;
+  fill_phase(d.ph[0], M, +1.f, (int)M, 1, 1, 0, t.S_log2);
+  fill_phase(d.ph[1], M, -1.f, (int)M, 1, 1, 0, t.S_log2);
+  d.nph = 2;
+  d.vec_a = cr.chirp;
+  d.vec_b = cr.spec;
+  d.in = io_of(in);
+  d.out = io_of(out);
+  d.in.line_fast = d.out.line_fast = 0;
+  s.lines = lines;
+  finish_geometry(s, M, false);
+  return s;
+}
+
+static TileStep single_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  if (gt_tile_ok(nd)) return gt_step(res, nd, sign, lines, in, out);
+  if (rader_tile_ok(nd)) return rader_step(res, nd, sign, lines, in, out);
+  if (chirp_tile_ok(nd)) return chirp_step(res, nd, sign, lines, in, out);
+  return plain_step(res, nd->n, sign, lines, in, out);
+}
+
+// ------------------------------------------------------- multi-pass schemes
+// A transform of length n too large for one tile runs as 2 or 3 passes over
+// a workspace region of `ws_len` elements per transform.  Views are built
+// for `T` transforms whose input/output rows are `xs` apart and whose
+// workspace regions are `wst` apart (the batch path places each transform
+// with per-item offsets and uses T = 1).
+struct MultiPass {
+  std::vector<TileStep> steps;
+  i64 ws_len = 0;
+};
+
+// Cooley-Tukey four-step (Planned.hs:525-557 for composite nodes; the
+// split-radix chain of Planned.hs:490-522 for even sizes): pass A FFT_n1 over
+// columns x[n2 j1 + j2] with twiddle W_n^(j2 k1), pass B FFT_n2 over rows,
+// X[k1 + n1 k2].
+static bool four_step_plan(PlanRes& res, i64 n, float sign, i64 T, i64 wst, const View& inb,
+                           const View& outb, i64 ws_base, MultiPass* mp) {
+  i64 n1, n2;
+  if (!four_step_split(n, &n1, &n2)) return false;
+  View a_in = inb;
+  a_in.s_e = n2 * inb.s_e; a_in.s_lo = inb.s_e; a_in.lo_cnt = n2;
+  View w;
+  w.buf = BUF_WS; w.off = ws_base; w.s_e = n2; w.s_lo = 1; w.s_hi = wst; w.lo_cnt = n2;
+  mp->steps.push_back(plain_step(res, n1, sign, T * n2, a_in, w, n));
+  View b_in;
+  b_in.buf = BUF_WS; b_in.off = ws_base; b_in.s_e = 1; b_in.s_lo = n2; b_in.s_hi = wst; b_in.lo_cnt = n1;
+  View b_out = outb;
+  b_out.s_e = n1 * outb.s_e; b_out.s_lo = outb.s_e; b_out.lo_cnt = n1;
+  mp->steps.push_back(plain_step(res, n2, sign, T * n1, b_in, b_out));
+  mp->ws_len = n;
+  return true;
+}
+
+// Good-Thomas in two passes (Planned.hs:584-617): pass 1 FFT_n over the CRT
+// gather x[(n k + m j) mod N] (line k, element j), stored transposed; pass 2
+// FFT_m over rows, scattered by the CRT map r = CRT(q, p).
+static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+                             const View& outb, i64 ws_base, MultiPass* mp) {
+  const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
+  if (!tile_ok(n) || !tile_ok(m)) return false;
+  View in1 = inb;
+  in1.lo_cnt = m;
+  View w1;
+  w1.buf = BUF_WS; w1.off = ws_base; w1.s_e = m; w1.s_lo = 1; w1.s_hi = wst; w1.lo_cnt = m;
+  TileStep s1 = plain_step(res, n, sign, T * m, in1, w1);
+  s1.d.in.map = IO_GT;
+  s1.d.in.mA = n; s1.d.in.mB = m; s1.d.in.mN = N; s1.d.in.s_t = inb.s_e;
+  s1.d.in.line_fast = 0;
+  mp->steps.push_back(s1);
+  View w2;
+  w2.buf = BUF_WS; w2.off = ws_base; w2.s_e = 1; w2.s_lo = m; w2.s_hi = wst; w2.lo_cnt = n;
+  View out2 = outb;
+  out2.lo_cnt = n;
+  TileStep s2 = plain_step(res, m, sign, T * n, w2, out2);
+  s2.d.out.map = IO_GT;
+  s2.d.out.mA = m * mod_inverse(m, n); s2.d.out.mB = n * mod_inverse(n, m); s2.d.out.mN = N;
+  s2.d.out.s_t = outb.s_e;
+  s2.d.out.line_fast = 0;
+  mp->steps.push_back(s2);
+  mp->ws_len = N;
+  return true;
+}
+
+// Cyclic convolution of length M = n1 n2 in three passes (Planned.hs:803-821,
+// directions as in the reference: G = sign +1 first, F = sign -1 after the
+// spectrum product):
+//   A   columns: FFT_n1(+1) over j1 of a[n2 j1 + j2], twiddle W_M^(+j2 k1)
+//   R   rows:    FFT_n2(+1), * S[k1 + n1 k2], FFT_n2(-1), twiddle W_M^(-j2 k1)
+//   A'  columns: FFT_n1(-1) over k1 -> c[n2 j1 + j2]
+// The load of A and the store of A' carry the Rader or Bluestein maps.
+static bool conv_plan(PlanRes& res, i64 M, const float2* S, i64 T, i64 wst, const View& inb,
+                      const View& outb, i64 ws_base, MultiPass* mp, TileStep** a_step, TileStep** o_step,
+                      i64 dc_off) {
+  i64 n1, n2;
+  if (!four_step_split(M, &n1, &n2)) return false;
+  View a_in = inb;
+  a_in.s_e = n2 * inb.s_e; a_in.s_lo = inb.s_e; a_in.lo_cnt = n2;
+  View w;
+  w.buf = BUF_WS; w.off = ws_base; w.s_e = n2; w.s_lo = 1; w.s_hi = wst; w.lo_cnt = n2;
+  mp->steps.push_back(plain_step(res, n1, +1.f, T * n2, a_in, w, M));
+  // rows
+  View r;
+  r.buf = BUF_WS; r.off = ws_base; r.s_e = 1; r.s_lo = n2; r.s_hi = wst; r.lo_cnt = n1;
+  TileStep rs = plain_step(res, n2, +1.f, T * n1, r, r, M);
+  rs.d.kind = TILE_CONVROW;
+  fill_phase(rs.d.ph[1], n2, -1.f, (int)n2, 1, 1, 0, rs.d.ph[0].twS_log2);
+  rs.d.nph = 2;
+  rs.d.vec_b = S;
+  rs.d.sq_lo = 1;
+  rs.d.sq_e = n1;
+  rs.d.ptw_sign = -1.f;
+  rs.d.dc_off = dc_off;
+  rs.d.in.line_fast = rs.d.out.line_fast = 0;
+  mp->steps.push_back(rs);
+  // columns back
+  View c_in;
+  c_in.buf = BUF_WS; c_in.off = ws_base; c_in.s_e = n2; c_in.s_lo = 1; c_in.s_hi = wst; c_in.lo_cnt = n2;
+  View c_out = outb;
+  c_out.s_e = n2 * outb.s_e; c_out.s_lo = outb.s_e; c_out.lo_cnt = n2;
+  mp->steps.push_back(plain_step(res, n1, -1.f, T * n2, c_in, c_out));
+  *a_step = &mp->steps[0];
+  *o_step = &mp->steps[2];
+  mp->ws_len = M + 1;  // batch regions (T = 1) keep their DC slot at offset M
+  return true;
+}
+
+// Rader in three passes: the conv of length M with the dlog gather/scatter
+// fused into the first load and the last store (x0 and DC fix-up included).
+static bool rader_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+                            const View& outb, i64 ws_base, MultiPass* mp) {
+  const i64 p = nd->n;
+  const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
+  const i64 M = rr.M, m = p - 1;
+  TileStep *a, *o;
+  // DC slots of the T transforms follow their T workspace regions
+  const i64 dc = ws_base + T * wst;
+  if (!conv_plan(res, M, rr.zs, T, wst, inb, outb, ws_base, mp, &a, &o, dc)) return false;
+  i64 n1, n2;
+  four_step_split(M, &n1, &n2);
+  // A: a[q] = x[g^-q] for q < p-1, zero beyond; q = n2 j1 + j2 = lo + n2 e
+  a->d.in.map = IO_TABLE;
+  a->d.in.tab = rr.src;
+  a->d.in.q_lo = 1; a->d.in.q_e = n2;
+  a->d.in.mN = m;
+  a->d.in.s_t = inb.s_e;
+  a->d.in.line_fast = 0;
+  // A': out[g^q] = x0 + c[q] for q < p-1; q == 0 also out[0] = x0 + DC
+  o->d.out.map = IO_RADER;
+  o->d.out.tab = rr.gpow;
+  o->d.out.q_lo = 1; o->d.out.q_e = n2;
+  o->d.out.mN = m;
+  o->d.out.s_t = outb.s_e;
+  o->d.out.x0_buf = inb.buf;
+  o->d.out.x0_off = inb.off;
+  o->d.out.x0_shi = inb.s_hi;
+  o->d.out.dc_off = dc;
+  o->d.out.line_fast = 0;
+  mp->ws_len = M + 1;
+  return true;
+}
+
+// Bluestein in three passes: chirp * x (zero padded) fused into the first
+// load, chirp * take N into the last store.
+static bool chirp_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+                            const View& outb, i64 ws_base, MultiPass* mp) {
+  const i64 N = nd->n, M = nd->a->n;
+  const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
+  TileStep *a, *o;
+  if (!conv_plan(res, M, cr.spec, T, wst, inb, outb, ws_base, mp, &a, &o, -1)) return false;
+  i64 n1, n2;
+  four_step_split(M, &n1, &n2);
+  a->d.in.map = IO_CHIRP;
+  a->d.in.vec = cr.chirp;
+  a->d.in.q_lo = 1; a->d.in.q_e = n2;
+  a->d.in.mN = N;
+  a->d.in.s_t = inb.s_e;
+  a->d.in.line_fast = 0;
+  o->d.out.map = IO_CHIRP;
+  o->d.out.vec = cr.chirp;
+  o->d.out.q_lo = 1; o->d.out.q_e = n2;
+  o->d.out.mN = N;
+  o->d.out.s_t = outb.s_e;
+  o->d.out.line_fast = 0;
+  mp->ws_len = M;
+  return true;
+}
+
+// Multi-pass scheme of a node: SR chains and composites as four-step,
+// coprime nodes as two-pass Good-Thomas, primes as three-pass Rader, chirp
+// nodes as three-pass Bluestein.
+// inb/outb: single-level views whose s_hi is the stride between transforms.
+static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+                       const View& outb, i64 ws_base, MultiPass* mp) {
+  switch (nd->kind) {
+    case N_COPRIME:
+      if (gt_two_pass_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp)) return true;
+      mp->steps.clear();
+      return four_step_plan(res, nd->n, sign, T, wst, inb, outb, ws_base, mp);
+    case N_PRIME: return rader_conv_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp);
+    case N_CHIRP: return chirp_conv_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp);
+    default: return four_step_plan(res, nd->n, sign, T, wst, inb, outb, ws_base, mp);
+  }
+}
+
+// workspace stride of a transform's multi-pass scheme
+static i64 multi_pass_len(const Node* nd) {
+  if (nd->kind == N_PRIME) return rader_conv_len(nd->n);
+  if (nd->kind == N_CHIRP) return nd->a->n;
+  return nd->n;
+}
+
+// ============================================================ programs
+static Launch launch_of(const TileStep& s) {
+  Launch L;
+  L.type = L_TILE;
+  L.descs.push_back(s.d);
+  L.threads = s.threads;
+  for (i64 l0 = 0; l0 < s.lines; l0 += s.d.G) {
+    WorkItem w;
+    memset(&w, 0, sizeof w);
+    w.desc = 0;
+    w.line0 = (int)l0;
+    w.G = (int)std::min<i64>(s.d.G, s.lines - l0);
+    L.items.push_back(w);
+  }
+  L.smem_data = spad_host(s.d.G * s.d.LS) + 2;
+  L.tw_max = s.d.tw_total;
+  L.g_max = s.d.G;
+  return L;
+}
+
+static void append_tile(Launch& L, const TileStep& s, int desc_index, i64 in_add, i64 out_add) {
+  for (i64 l0 = 0; l0 < s.lines; l0 += s.d.G) {
+    WorkItem w;
+    memset(&w, 0, sizeof w);
+    w.desc = desc_index;
+    w.line0 = (int)l0;
+    w.G = (int)std::min<i64>(s.d.G, s.lines - l0);
+    w.in_add = in_add;
+    w.out_add = out_add;
+    L.items.push_back(w);
+  }
+  L.smem_data = std::max(L.smem_data, spad_host(s.d.G * s.d.LS) + 2);
+  L.tw_max = std::max(L.tw_max, s.d.tw_total);
+  L.g_max = std::max(L.g_max, s.d.G);
+  L.threads = std::max(L.threads, s.threads);
+}
+
+int Program::tile_launches() const { return (int)launches.size(); }
+
+void finalize_program(PlanRes& res, Program& prog) {
+  size_t bytes = 0;
+  for (Launch& L : prog.launches) {
+    if (L.type != L_TILE) continue;
+    bytes = (bytes + 255) / 256 * 256;
+    L.desc_off = bytes;
+    bytes += sizeof(TileDesc) * L.descs.size();
+    bytes = (bytes + 255) / 256 * 256;
+    L.item_off = bytes;
+    bytes += sizeof(WorkItem) * L.items.size();
+  }
+  if (!bytes) return;
+  std::vector<char> host(bytes, 0);
+  for (Launch& L : prog.launches) {
+    if (L.type != L_TILE) continue;
+    memcpy(host.data() + L.desc_off, L.descs.data(), sizeof(TileDesc) * L.descs.size());
+    memcpy(host.data() + L.item_off, L.items.data(), sizeof(WorkItem) * L.items.size());
+  }
+  prog.dblob = (char*)res.dalloc(bytes);
+  cuda_check(cudaMemcpy(prog.dblob, host.data(), bytes, cudaMemcpyHostToDevice), "program upload");
+}
+
+TileBases make_bases(const float* in_re, const float* in_im, float* out_re, float* out_im, float2* ws,
+                     const float* aux_re, const float* aux_im) {
+  TileBases b;
+  memset(&b, 0, sizeof b);
+  if (in_im) { b.re[BUF_IN] = (float*)in_re; b.im[BUF_IN] = (float*)in_im; }
+  else b.c[BUF_IN] = (float2*)in_re;
+  if (out_im) { b.re[BUF_OUT] = out_re; b.im[BUF_OUT] = out_im; }
+  else b.c[BUF_OUT] = (float2*)out_re;
+  b.c[BUF_WS] = ws;
+  if (aux_im) { b.re[BUF_AUX] = (float*)aux_re; b.im[BUF_AUX] = (float*)aux_im; }
+  else b.c[BUF_AUX] = (float2*)aux_re;
+  return b;
+}
+
+cudaError_t run_program(const Program& prog, const TileBases& bases, double* loss, cudaStream_t st) {
+  for (const Launch& L : prog.launches) {
+    cudaError_t e;
+    if (L.type == L_TILE) {
+      LaunchSpec spec;
+      spec.descs = reinterpret_cast<const TileDesc*>(prog.dblob + L.desc_off);
+      spec.items = reinterpret_cast<const WorkItem*>(prog.dblob + L.item_off);
+      spec.nitems = (int)L.items.size();
+      spec.threads = L.threads;
+      spec.smem_data = L.smem_data;
+      spec.smem_bytes = tile_smem_bytes(L.smem_data, L.tw_max, L.g_max);
+      e = launch_tiles(spec, bases, loss, st);
+    } else {
+      e = launch_map(L.md, bases, st);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ============================================================ single-plan lowering
 struct Lowering {
-  af_plan_s* P;
+  PlanRes& res;
   Program* prog;
   i64 top = 0;
   i64 peak = 0;
@@ -280,29 +785,20 @@ struct Lowering {
     peak = std::max(peak, top);
     return o;
   }
-
   static bool simple(const View& v, i64 lines) { return v.lo_cnt >= lines; }
 
-  void emit_tile(const TileDesc& td, int threads, const View& in, const View& out) {
-    Step s;
-    s.type = STEP_TILE;
-    s.td = td;
-    s.threads = threads;
-    s.vin = in;
-    s.vout = out;
-    prog->steps.push_back(s);
+  void emit_step(const TileStep& s) { prog->launches.push_back(launch_of(s)); }
+
+  void emit_map(MapDesc md, const View& in, const View& out) {
+    Launch L;
+    L.type = L_MAP;
+    md.in = io_of(in);
+    md.out = io_of(out);
+    L.md = md;
+    prog->launches.push_back(L);
   }
 
-  void emit_map(const MapDesc& md, const View& in, const View& out) {
-    Step s;
-    s.type = STEP_MAP;
-    s.md = md;
-    s.vin = in;
-    s.vout = out;
-    prog->steps.push_back(s);
-  }
-
-  MapDesc map0(int mode, i64 lines, i64 nout) {
+  static MapDesc map0(int mode, i64 lines, i64 nout) {
     MapDesc m;
     memset(&m, 0, sizeof m);
     m.mode = mode;
@@ -314,226 +810,68 @@ struct Lowering {
     return m;
   }
 
-  // plain tile: FFT of length n over `lines` lines with optional four-step twiddle
-  void plain_tile(i64 n, float sign, i64 lines, const View& in, const View& out, i64 ptwN = 0,
-                  float scale = 1.f) {
-    TileDesc td;
-    memset(&td, 0, sizeof td);
-    td.kind = TILE_PLAIN;
-    td.nlen = (int)n;
-    td.nlines = (int)lines;
-    td.slen = (int)n;
-    td.LS = (int)n;
-    TwTable t = P->res.table(n);
-    td.tw_src = t.p;
-    td.tw_total = t.len;
-    fill_phase(td.ph[0], n, sign, (int)n, 1, 1, 0, t.S_log2);
-    td.nph = 1;
-    td.in = io_of(in);
-    td.out = io_of(out);
-    td.scale = scale;
-    if (ptwN) {
-      TwTable pt = P->res.table(ptwN);
-      td.ptw = pt.p;
-      td.ptwS_log2 = pt.S_log2;
-      td.ptwN = ptwN;
-      td.ptw_col_mul = 1;
-      td.ptw_sign = sign;
-    }
-    int threads, G;
-    choose_geometry(n, lines, td.tw_total, td.in.line_fast || td.out.line_fast, &threads, &G);
-    td.G = G;
-    td.N_div = make_fastdiv((unsigned)n);
-    td.S_div = td.N_div;
-    td.G_div = make_fastdiv((unsigned)G);
-    emit_tile(td, threads, in, out);
-  }
-
-  bool gt_tile_ok(const Node* nd) {
-    return nd->kind == N_COPRIME && nd->n <= kTileCap && tile_ok(nd->a->n) && tile_ok(nd->b->n);
-  }
-  bool rader_tile_ok(const Node* nd) { return nd->kind == N_PRIME && nd->n > 13 && tile_ok(nd->n - 1); }
-  bool chirp_tile_ok(const Node* nd) { return nd->kind == N_CHIRP && tile_ok(nd->a->n); }
-
-  // Good-Thomas tile (Planned.hs:584-617): grid m x n, n = first factor
-  void gt_tile(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
-    const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
-    TileDesc td;
-    memset(&td, 0, sizeof td);
-    td.kind = TILE_GT;
-    td.nlen = (int)N;
-    td.nlines = (int)lines;
-    td.slen = (int)N;
-    td.LS = (int)N;
-    int offb = 0;
-    td.tw_src = P->res.pair_table(n, m, &offb);
-    td.tw_total = P->res.table(n).len + P->res.table(m).len;
-    fill_phase(td.ph[0], n, sign, (int)n, 1, (int)m, 0, P->res.table(n).S_log2);       // rows (j)
-    fill_phase(td.ph[1], m, sign, 1, (int)n, (int)n, offb, P->res.table(m).S_log2);    // cols (k)
-    td.nph = 2;
-    td.gt_n = (int)n;
-    td.gt_m = (int)m;
-    // i = (n k + m j) mod N  =>  k = i * n^-1 mod m,  j = i * m^-1 mod n
-    td.gt_cm = mod_inverse(n % m, m);
-    td.gt_cn = mod_inverse(m % n, n);
-    td.in = io_of(in);
-    td.out = io_of(out);
-    td.in.line_fast = 0;
-    td.out.line_fast = 0;
-    td.scale = 1.f;
-    int threads, G;
-    choose_geometry(N, lines, td.tw_total, false, &threads, &G);
-    td.G = G;
-    td.N_div = make_fastdiv((unsigned)N);
-    td.S_div = td.N_div;
-    td.G_div = make_fastdiv((unsigned)G);
-    emit_tile(td, threads, in, out);
-  }
-
-  static i64 mod_inverse(i64 a, i64 m) {
-    if (m == 1) return 0;
-    // extended Euclid
-    i64 t = 0, nt = 1, r = m, nr = a % m;
-    while (nr) {
-      i64 q = r / nr;
-      i64 tmp = t - q * nt; t = nt; nt = tmp;
-      tmp = r - q * nr; r = nr; nr = tmp;
-    }
-    return t < 0 ? t + m : t;
-  }
-
-  // Rader tile (Planned.hs:646-692)
-  void rader_tile(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
-    const i64 p = nd->n, m = p - 1;
-    const RaderRes& rr = P->res.rader_res(p, sign > 0 ? 1 : -1);
-    TileDesc td;
-    memset(&td, 0, sizeof td);
-    td.kind = TILE_RADER;
-    td.nlen = (int)p;
-    td.nlines = (int)lines;
-    td.slen = (int)m;
-    td.LS = (int)m;
-    TwTable t = P->res.table(m);
-    td.tw_src = t.p;
-    td.tw_total = t.len;
-    fill_phase(td.ph[0], m, +1.f, (int)m, 1, 1, 0, t.S_log2);
-    fill_phase(td.ph[1], m, -1.f, (int)m, 1, 1, 0, t.S_log2);
-    td.nph = 2;
-    td.dlog = rr.dlog;
-    td.vec_b = rr.zs;
-    td.in = io_of(in);
-    td.out = io_of(out);
-    td.in.line_fast = 0;
-    td.out.line_fast = 0;
-    td.scale = 1.f;
-    int threads, G;
-    choose_geometry(m, lines, td.tw_total, false, &threads, &G);
-    td.G = G;
-    td.N_div = make_fastdiv((unsigned)p);
-    td.S_div = make_fastdiv((unsigned)m);
-    td.G_div = make_fastdiv((unsigned)G);
-    emit_tile(td, threads, in, out);
-  }
-
-  // Bluestein tile (Planned.hs:760-773)
-  void chirp_tile(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
-    const i64 N = nd->n, M = nd->a->n;
-    const ChirpRes& cr = P->res.chirp_res(N, M, sign > 0 ? 1 : -1);
-    TileDesc td;
-    memset(&td, 0, sizeof td);
-    td.kind = TILE_BLUESTEIN;
-    td.nlen = (int)N;
-    td.nlines = (int)lines;
-    td.slen = (int)M;
-    td.LS = (int)M;
-    TwTable t = P->res.table(M);
-    td.tw_src = t.p;
-    td.tw_total = t.len;
-    fill_phase(td.ph[0], M, +1.f, (int)M, 1, 1, 0, t.S_log2);
-    fill_phase(td.ph[1], M, -1.f, (int)M, 1, 1, 0, t.S_log2);
-    td.nph = 2;
-    td.vec_a = cr.chirp;
-    td.vec_b = cr.spec;
-    td.in = io_of(in);
-    td.out = io_of(out);
-    td.in.line_fast = 0;
-    td.out.line_fast = 0;
-    td.scale = 1.f;
-    int threads, G;
-    choose_geometry(M, lines, td.tw_total, false, &threads, &G);
-    td.G = G;
-    td.N_div = make_fastdiv((unsigned)N);
-    td.S_div = make_fastdiv((unsigned)M);
-    td.G_div = make_fastdiv((unsigned)G);
-    emit_tile(td, threads, in, out);
-  }
-
-  bool tileable(const Node* nd) {
-    if (nd->n <= 1) return true;
-    if (gt_tile_ok(nd) || rader_tile_ok(nd) || chirp_tile_ok(nd)) return true;
-    return tile_ok(nd->n) && nd->kind != N_CHIRP && !(nd->kind == N_PRIME && nd->n > 13);
-  }
-
-  // ---------------------------------------------------------------- node
   // Transform `lines` rows through any 2-level views.
   void node(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
     const i64 n = nd->n;
     if (n == 0 || lines == 0) return;
     if (n == 1) {
-      MapDesc md = map0(MAP_COPY, lines, 1);
-      emit_map(md, in, out);
+      emit_map(map0(MAP_COPY, lines, 1), in, out);
       return;
     }
-    if (gt_tile_ok(nd)) { gt_tile(nd, sign, lines, in, out); return; }
-    if (rader_tile_ok(nd)) { rader_tile(nd, sign, lines, in, out); return; }
-    if (chirp_tile_ok(nd)) { chirp_tile(nd, sign, lines, in, out); return; }
-    if (tile_ok(n) && nd->kind != N_CHIRP && !(nd->kind == N_PRIME && n > 13)) {
-      plain_tile(n, sign, lines, in, out);
+    if (single_tile_ok(nd)) {
+      emit_step(single_step(res, nd, sign, lines, in, out));
       return;
     }
-    // multi-launch structures need single-level views; route others via temps
+    // multi-pass schemes need single-level views; route others via temps
     if (!simple(in, lines) || !simple(out, lines)) {
       const i64 mark = top;
       View tin = in, tout = out;
       if (!simple(in, lines)) {
         tin = View::rows(BUF_WS, alloc(lines * n), n, lines);
-        MapDesc md = map0(MAP_COPY, lines, n);
-        emit_map(md, in, tin);
+        emit_map(map0(MAP_COPY, lines, n), in, tin);
       }
       if (!simple(out, lines)) tout = View::rows(BUF_WS, alloc(lines * n), n, lines);
       node(nd, sign, lines, tin, tout);
-      if (!simple(out, lines)) {
-        MapDesc md = map0(MAP_COPY, lines, n);
-        emit_map(md, tout, out);
-      }
+      if (!simple(out, lines)) emit_map(map0(MAP_COPY, lines, n), tout, out);
       top = mark;
       return;
+    }
+    // fused multi-pass scheme over all rows
+    {
+      MultiPass mp;
+      const i64 mark = top;
+      const i64 wsr = multi_pass_len(nd);
+      const i64 W = alloc(lines * wsr + lines + 64);
+      View inb = in, outb = out;
+      inb.s_hi = in.s_lo; inb.s_lo = 0; inb.lo_cnt = 1;
+      outb.s_hi = out.s_lo; outb.s_lo = 0; outb.lo_cnt = 1;
+      if (multi_pass(res, nd, sign, lines, wsr, inb, outb, W, &mp)) {
+        for (auto& s : mp.steps) emit_step(s);
+        top = mark;
+        return;
+      }
+      top = mark;
     }
     switch (nd->kind) {
       case N_COPRIME: good_thomas(nd, sign, lines, in, out); return;
       case N_PRIME: rader_multi(nd, sign, lines, in, out); return;
       case N_CHIRP: bluestein_multi(nd, sign, lines, in, out); return;
-      default: four_step(nd, sign, lines, in, out); return;
+      default: recursive_four_step(nd, sign, lines, in, out); return;
     }
   }
 
-  // Cooley-Tukey four-step for SR chains and composite nodes:
-  // n = n1 * n2, x[n2 j1 + j2]; pass A: FFT_n1 over j1 (+ twiddle W_n^(j2 k1));
-  // pass B: FFT_n2 over j2; X[k1 + n1 k2].  (Planned.hs:490-557)
-  void four_step(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  // Cooley-Tukey four-step with a recursive row transform (sizes whose rows
+  // do not fit one tile): columns n1 = power of two from the SR chain or the
+  // composite's first factor.
+  void recursive_four_step(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
     const i64 n = nd->n;
     i64 n1;
     const Node* sub2;
     if (nd->kind == N_SR) {
       int a = 0;
       const Node* c = nd;
-      std::vector<const Node*> chain;
-      while (c->kind == N_SR) { chain.push_back(c); c = c->a; ++a; }
-      const int lg = ceil_log2(n);
-      int k = (lg + 1) / 2;
-      k = std::max(k, ceil_log2((n + kTileCap - 1) / kTileCap));
-      k = std::min(k, std::min(a, 10));
-      k = std::max(k, 1);
+      while (c->kind == N_SR) { c = c->a; ++a; }
+      int k = std::min(a, 10);
       n1 = (i64)1 << k;
       sub2 = nd;
       for (int i = 0; i < k; ++i) sub2 = sub2->a;
@@ -546,7 +884,6 @@ struct Lowering {
     const i64 n2 = n / n1;
     const i64 mark = top;
     const i64 W = alloc(lines * n);
-    // pass A
     View a_in;
     a_in.buf = in.buf; a_in.off = in.off;
     a_in.s_e = n2 * in.s_e; a_in.s_lo = in.s_e; a_in.s_hi = in.s_lo; a_in.lo_cnt = n2;
@@ -554,27 +891,22 @@ struct Lowering {
     a_out.buf = BUF_WS; a_out.off = W;
     a_out.s_e = n2; a_out.s_lo = 1; a_out.s_hi = n; a_out.lo_cnt = n2;
     if (tile_ok(n1)) {
-      plain_tile(n1, sign, lines * n2, a_in, a_out, n);
+      emit_step(plain_step(res, n1, sign, lines * n2, a_in, a_out, n));
     } else {
-      // columns that need a multi-launch transform: transpose, transform, twiddle
       const i64 T1 = alloc(lines * n), T2 = alloc(lines * n);
       View trows = View::rows(BUF_WS, T1, n1, lines * n2);
-      MapDesc cp = map0(MAP_COPY, lines * n2, n1);
-      emit_map(cp, a_in, trows);
+      emit_map(map0(MAP_COPY, lines * n2, n1), a_in, trows);
       View t2rows = View::rows(BUF_WS, T2, n1, lines * n2);
       node(nd->a, sign, lines * n2, trows, t2rows);
-      MapDesc tw = map0(MAP_MUL, lines * n2, n1);
-      tw.vec = nullptr;
+      MapDesc tw = map0(MAP_TWIDDLE, lines * n2, n1);
       tw.n = n;
-      tw.m = n2;  // column = line % n2
-      tw.mode = MAP_TWIDDLE;
-      TwTable pt = P->res.table(n);
+      tw.m = n2;
+      TwTable pt = res.table(n);
       tw.tab_tw = pt.p;
       tw.tw_log2 = pt.S_log2;
       tw.tw_sign = sign;
       emit_map(tw, t2rows, a_out);
     }
-    // pass B: rows of W -> out[k1 + n1 k2]
     View b_in = View::rows(BUF_WS, W, n2, lines * n1);
     View b_out;
     b_out.buf = out.buf; b_out.off = out.off;
@@ -588,17 +920,14 @@ struct Lowering {
     const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
     const i64 mark = top;
     const i64 W1 = alloc(lines * N), W2 = alloc(lines * N);
-    View w1 = View::rows(BUF_WS, W1, N, lines);
     MapDesc g = map0(MAP_GT_IN, lines, N);
     g.n = n; g.m = m; g.nm = N;
-    emit_map(g, in, w1);
-    // FFT_n along rows of the m x n grid, stored transposed (n x m)
+    emit_map(g, in, View::rows(BUF_WS, W1, N, lines));
     View r_in = View::rows(BUF_WS, W1, n, lines * m);
     View r_out;
     r_out.buf = BUF_WS; r_out.off = W2;
     r_out.s_e = m; r_out.s_lo = 1; r_out.s_hi = N; r_out.lo_cnt = m;
     node(nd->a, sign, lines * m, r_in, r_out);
-    // FFT_m along rows of the transposed grid
     View c_in = View::rows(BUF_WS, W2, m, lines * n);
     View c_out = View::rows(BUF_WS, W1, m, lines * n);
     node(nd->b, sign, lines * n, c_in, c_out);
@@ -608,10 +937,12 @@ struct Lowering {
     top = mark;
   }
 
-  // Rader through explicit permutation maps (Planned.hs:646-692)
+  // Rader through explicit permutation maps and the sub-plan of p-1
+  // (Planned.hs:646-692); used only when p-1 has no fused scheme
   void rader_multi(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
     const i64 p = nd->n, m = p - 1;
-    const RaderRes& rr = P->res.rader_res(p, sign > 0 ? 1 : -1);
+    const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
+    if (rr.M != m) throw AfError(AF_ERR_UNSUPPORTED, "Rader length without a fused scheme");
     const i64 mark = top;
     const i64 W1 = alloc(lines * m), W2 = alloc(lines * m), X0 = alloc(lines), DC = alloc(lines);
     View w1 = View::rows(BUF_WS, W1, m, lines), w2 = View::rows(BUF_WS, W2, m, lines);
@@ -636,7 +967,7 @@ struct Lowering {
   // Bluestein through explicit chirp maps (Planned.hs:760-773)
   void bluestein_multi(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
     const i64 N = nd->n, M = nd->a->n;
-    const ChirpRes& cr = P->res.chirp_res(N, M, sign > 0 ? 1 : -1);
+    const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
     const i64 mark = top;
     const i64 W1 = alloc(lines * M), W2 = alloc(lines * M);
     View w1 = View::rows(BUF_WS, W1, M, lines), w2 = View::rows(BUF_WS, W2, M, lines);
@@ -656,56 +987,214 @@ struct Lowering {
   }
 };
 
-// ============================================================ plan object
-void build_program(af_plan_s* P, const Node* root, float sign, i64 batch, Program* prog) {
-  Lowering L{P, prog};
-  prog->steps.clear();
+void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Program* prog) {
+  Lowering L{res, prog};
+  prog->launches.clear();
   View in = View::rows(BUF_IN, 0, root->n, batch);
   View out = View::rows(BUF_OUT, 0, root->n, batch);
   L.node(root, sign, batch, in, out);
   prog->ws_elems = L.peak;
+  finalize_program(res, *prog);
 }
 
-static IoDesc resolve(const View& v, const ExecBufs& b) {
-  IoDesc io = io_of(v);
-  switch (v.buf) {
-    case BUF_IN:
-      if (b.in_im) { io.re = (float*)b.in_re + v.off; io.im = (float*)b.in_im + v.off; }
-      else io.c = (float2*)b.in_re + v.off;
-      break;
-    case BUF_OUT:
-      if (b.out_im) { io.re = b.out_re + v.off; io.im = b.out_im + v.off; }
-      else io.c = (float2*)b.out_re + v.off;
-      break;
-    default:
-      io.c = b.ws + v.off;
-      break;
-  }
-  return io;
-}
+// ============================================================ batched executor
+// Many transforms of mixed lengths stored back to back.  Every transform is
+// planned with the reference planner; transforms that fit one tile run in
+// a handful of launches (split by CTA size), larger ones run their fused
+// multi-pass scheme, with the transforms grouped into chunks whose
+// workspace stays resident in L2 between passes.
+struct BatchPlan {
+  i64 count = 0;
+  int sign = -1;
+  std::vector<i64> ns, offs;
+  Planner planner;
+  PlanRes res;
+  Program fwd, inv, cot;  // sign, -sign, sign with the cotangent epilogue
+  i64 ws_elems = 0;
+  float2* ws = nullptr;
+  i64 fallback = 0;      // transforms executed through their own programs
+  bool cot_ok = true;    // every transform has a fused program for the cotangent epilogue
+  std::vector<std::pair<i64, Program>> fb_fwd, fb_inv;  // (index, program)
+};
 
-cudaError_t run_program(const Program& prog, const ExecBufs& b, cudaStream_t st) {
-  for (const Step& s : prog.steps) {
-    cudaError_t e;
-    if (s.type == STEP_TILE) {
-      TileDesc td = s.td;
-      const int lf_in = td.in.line_fast, lf_out = td.out.line_fast;
-      td.in = resolve(s.vin, b);
-      td.out = resolve(s.vout, b);
-      td.in.line_fast = lf_in;
-      td.out.line_fast = lf_out;
-      e = launch_tile(td, s.threads, st);
-    } else {
-      MapDesc md = s.md;
-      md.in = resolve(s.vin, b);
-      md.out = resolve(s.vout, b);
-      if (md.x0_ws >= 0) md.x0 = b.ws + md.x0_ws;
-      if (md.dc_ws >= 0) md.dc = b.ws + md.dc_ws;
-      e = launch_map(md, st);
+static const i64 kChunkElems = (i64)6 << 20;  // 48 MB of workspace per L2 chunk
+
+static void build_batch_program(BatchPlan* B, float sign, Program& prog,
+                                std::vector<std::pair<i64, Program>>& fallback, bool cot) {
+  prog.launches.clear();
+  fallback.clear();
+  std::map<i64, const Node*> roots;
+  // stage 0: single-tile transforms, one launch per thread class
+  std::map<int, Launch> single;
+  std::map<std::pair<i64, int>, int> single_desc;  // (n, threads) -> desc index
+  struct Big {
+    i64 i;
+    MultiPass mp;
+  };
+  std::vector<Big> bigs;
+  for (i64 i = 0; i < B->count; ++i) {
+    const i64 n = B->ns[i];
+    if (n == 0) continue;
+    const Node* nd = B->planner.automatic(n);
+    View in = View::rows(BUF_IN, 0, n, 1), out = View::rows(BUF_OUT, 0, n, 1);
+    if (single_tile_ok(nd)) {
+      TileStep s = single_step(B->res, nd, sign, 1, in, out);
+      if (nd->n == 1) s = plain_step(B->res, 1, sign, 1, in, out);
+      s.d.cot = cot;
+      Launch& L = single[s.threads];
+      L.type = L_TILE;
+      auto key = std::make_pair(n, s.threads);
+      int di;
+      auto it = single_desc.find(key);
+      if (it == single_desc.end()) {
+        di = (int)L.descs.size();
+        L.descs.push_back(s.d);
+        single_desc[key] = di;
+      } else {
+        di = it->second;
+      }
+      append_tile(L, s, di, B->offs[i], B->offs[i]);
+      continue;
     }
+    Big b;
+    b.i = i;
+    View inb = in, outb = out;
+    inb.s_hi = n; inb.s_lo = 0; inb.lo_cnt = 1;
+    outb.s_hi = n; outb.s_lo = 0; outb.lo_cnt = 1;
+    if (multi_pass(B->res, nd, sign, 1, multi_pass_len(nd), inb, outb, 0, &b.mp)) {
+      b.mp.steps.back().d.cot = cot;
+      bigs.push_back(std::move(b));
+    } else {
+      Program p;
+      build_program(B->res, nd, sign, 1, &p);
+      fallback.emplace_back(i, std::move(p));
+    }
+  }
+  for (auto& kv : single) {
+    // heavy items first
+    std::stable_sort(kv.second.items.begin(), kv.second.items.end(),
+                     [&](const WorkItem& a, const WorkItem& b) {
+                       return kv.second.descs[a.desc].slen > kv.second.descs[b.desc].slen;
+                     });
+    prog.launches.push_back(kv.second);
+  }
+  // multi-pass transforms: chunks by workspace size, one launch per pass index
+  std::sort(bigs.begin(), bigs.end(), [](const Big& a, const Big& b) { return a.mp.ws_len > b.mp.ws_len; });
+  i64 peak = 0;
+  size_t k = 0;
+  while (k < bigs.size()) {
+    i64 used = 0;
+    size_t e = k;
+    while (e < bigs.size() && (e == k || used + bigs[e].mp.ws_len + 64 <= kChunkElems)) {
+      used += (bigs[e].mp.ws_len + 63) / 64 * 64 + 64;
+      ++e;
+    }
+    size_t maxsteps = 0;
+    for (size_t j = k; j < e; ++j) maxsteps = std::max(maxsteps, bigs[j].mp.steps.size());
+    for (size_t st = 0; st < maxsteps; ++st) {
+      Launch L;
+      L.type = L_TILE;
+      std::map<std::pair<i64, int>, int> dmap;
+      i64 wpos = 0;
+      for (size_t j = k; j < e; ++j) {
+        const Big& b = bigs[j];
+        const i64 woff = wpos;
+        wpos += (b.mp.ws_len + 63) / 64 * 64 + 64;
+        if (st >= b.mp.steps.size()) continue;
+        const TileStep& s = b.mp.steps[st];
+        const i64 n = B->ns[b.i];
+        auto key = std::make_pair(n, s.threads);
+        int di;
+        auto it = dmap.find(key);
+        if (it == dmap.end()) {
+          di = (int)L.descs.size();
+          L.descs.push_back(s.d);
+          dmap[key] = di;
+        } else {
+          di = it->second;
+        }
+        // in: user input (pass 0) or workspace; out: workspace or user output
+        const i64 in_add = s.d.in.buf == BUF_WS ? woff : B->offs[b.i];
+        const i64 out_add = s.d.out.buf == BUF_WS ? woff : B->offs[b.i];
+        append_tile(L, s, di, in_add, out_add);
+      }
+      if (!L.items.empty()) prog.launches.push_back(L);
+      peak = std::max(peak, wpos);
+    }
+    k = e;
+  }
+  prog.ws_elems = peak;
+  finalize_program(B->res, prog);
+}
+
+BatchPlan* batch_create(const i64* ns, i64 count, int sign) {
+  BatchPlan* B = new BatchPlan();
+  try {
+    B->count = count;
+    B->sign = sign;
+    B->ns.assign(ns, ns + count);
+    B->offs.resize(count);
+    i64 o = 0;
+    for (i64 i = 0; i < count; ++i) {
+      if (ns[i] < 0) throw AfError(AF_ERR_INVALID, "negative transform length");
+      B->offs[i] = o;
+      o += ns[i];
+    }
+    if (o >= ((i64)1 << 31)) throw AfError(AF_ERR_UNSUPPORTED, "total length must be below 2^31");
+    build_batch_program(B, (float)sign, B->fwd, B->fb_fwd, false);
+    build_batch_program(B, (float)-sign, B->inv, B->fb_inv, false);
+    std::vector<std::pair<i64, Program>> fb_cot;
+    build_batch_program(B, (float)sign, B->cot, fb_cot, true);
+    B->cot_ok = fb_cot.empty();
+    i64 ws = std::max(std::max(B->fwd.ws_elems, B->inv.ws_elems), B->cot.ws_elems);
+    for (auto& f : B->fb_fwd) ws = std::max(ws, f.second.ws_elems);
+    for (auto& f : B->fb_inv) ws = std::max(ws, f.second.ws_elems);
+    B->fallback = (i64)B->fb_fwd.size();
+    B->ws_elems = ws;
+    if (ws) cuda_check(cudaMalloc(&B->ws, sizeof(float2) * ws), "batch workspace");
+    cuda_check(cudaDeviceSynchronize(), "batch tables");
+  } catch (...) {
+    batch_destroy(B);
+    throw;
+  }
+  return B;
+}
+
+void batch_destroy(BatchPlan* B) {
+  if (!B) return;
+  if (B->ws) cudaFree(B->ws);
+  B->res.release();
+  delete B;
+}
+
+cudaError_t batch_run(BatchPlan* B, bool inverse, const float2* in, float2* out, const float* w, double* loss,
+                      cudaStream_t st) {
+  if (w && !B->cot_ok) throw AfError(AF_ERR_UNSUPPORTED, "cotangent epilogue needs fused programs for every length");
+  const Program& prog = w ? B->cot : (inverse ? B->inv : B->fwd);
+  TileBases bases = make_bases((const float*)in, nullptr, (float*)out, nullptr, B->ws, w, nullptr);
+  if (w) {
+    // weights are real: BUF_AUX is read as a float plane indexed like the output
+    bases.c[BUF_AUX] = nullptr;
+    bases.re[BUF_AUX] = (float*)w;
+  }
+  cudaError_t e = run_program(prog, bases, loss, st);
+  if (e != cudaSuccess) return e;
+  if (w) return cudaSuccess;
+  for (auto& f : (inverse ? B->fb_inv : B->fb_fwd)) {
+    const i64 o = B->offs[f.first];
+    TileBases b2 = make_bases((const float*)(in + o), nullptr, (float*)(out + o), nullptr, B->ws,
+                              w ? w + o : nullptr, nullptr);
+    if (w) { b2.c[BUF_AUX] = nullptr; b2.re[BUF_AUX] = (float*)(w + o); }
+    e = run_program(f.second, b2, loss, st);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+i64 batch_launches(BatchPlan* B) {
+  i64 n = (i64)B->fwd.launches.size();
+  for (auto& f : B->fb_fwd) n += (i64)f.second.launches.size();
+  return n;
 }
 
 }  // namespace af

@@ -1,5 +1,5 @@
 // af_host.h -- host-side structures of libaf: plan resources, launch
-// programs, and the plan object behind the C ABI's af_plan handle.
+// programs, tile builders, and the objects behind the C ABI's handles.
 #pragma once
 #include <map>
 #include <stdexcept>
@@ -17,8 +17,6 @@ struct AfError : std::runtime_error {
   af_status code;
   AfError(af_status c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
-
-enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2 };
 
 // A batch of lines: line l = hi * lo_cnt + lo, element e at
 // off + hi*s_hi + lo*s_lo + e*s_e in buffer `buf` (complex units).
@@ -38,27 +36,25 @@ struct View {
   }
 };
 
-enum StepType { STEP_TILE = 0, STEP_MAP = 1 };
+enum LaunchType { L_TILE = 0, L_MAP = 1 };
 
-struct Step {
-  int type = STEP_TILE;
-  TileDesc td;
-  int threads = 256;
+struct Launch {
+  int type = L_TILE;
+  std::vector<TileDesc> descs;
+  std::vector<WorkItem> items;
+  int threads = 128;
+  int smem_data = 0;
+  int tw_max = 0;
+  int g_max = 0;
   MapDesc md;
-  View vin, vout;
+  size_t desc_off = 0, item_off = 0;  // byte offsets in the program's device blob
 };
 
 struct Program {
-  std::vector<Step> steps;
+  std::vector<Launch> launches;
   i64 ws_elems = 0;
-};
-
-struct ExecBufs {
-  const float* in_re;
-  const float* in_im;  // NULL for interleaved
-  float* out_re;
-  float* out_im;
-  float2* ws;
+  char* dblob = nullptr;  // device copy of every launch's descriptors and items
+  int tile_launches() const;
 };
 
 struct TwTable {
@@ -68,11 +64,14 @@ struct TwTable {
 
 struct RaderRes {
   i64 p = 0, g = 0;
-  int* dlog = nullptr;  // dlog[r-1] = log_g r
-  int* src = nullptr;   // src[q] = 1 + perm[(-q) mod (p-1)] = g^-q mod p
-  int* inv = nullptr;   // inverse permutation
-  float2* zs = nullptr; // kernel spectrum / (p-1)
+  int* dlog = nullptr;   // dlog[r-1] = log_g r
+  int* src = nullptr;    // src[q] = 1 + perm[(-q) mod (p-1)] = g^-q mod p
+  int* inv = nullptr;    // inverse permutation
+  int* gpow = nullptr;   // gpow[q] = g^q mod p (scatter target of conv index q)
+  float2* zs = nullptr;  // kernel spectrum / M (M entries)
+  i64 M = 0;             // conv transform length (rader_conv_len)
 };
+i64 rader_conv_len(i64 p);
 
 struct ChirpRes {
   i64 len = 0, pad = 0;
@@ -95,7 +94,18 @@ struct PlanRes {
 };
 
 bool tile_ok(i64 n);
-cudaError_t run_program(const Program& prog, const ExecBufs& b, cudaStream_t st);
+void finalize_program(PlanRes& res, Program& prog);
+cudaError_t run_program(const Program& prog, const TileBases& bases, double* loss, cudaStream_t st);
+TileBases make_bases(const float* in_re, const float* in_im, float* out_re, float* out_im, float2* ws,
+                     const float* aux_re, const float* aux_im);
+
+// Builds the launch program of one plan tree over `batch` contiguous rows.
+void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Program* prog);
+
+// Batched executor: many transforms of mixed lengths, concatenated.
+struct BatchPlan;
+BatchPlan* batch_create(const i64* ns, i64 count, int sign);
+void batch_destroy(BatchPlan* b);
 
 }  // namespace af
 
@@ -111,7 +121,3 @@ struct af_plan_s {
   size_t ws_elems = 0;
   ~af_plan_s();
 };
-
-namespace af {
-void build_program(af_plan_s* P, const Node* root, float sign, i64 batch, Program* prog);
-}

@@ -6,9 +6,20 @@
 
 namespace af {
 
+__host__ __device__ __forceinline__ int spad_host(int i) { return i + (i >> 4); }
+
 // ------------------------------------------------------------- tile kernel
-size_t tile_smem_bytes(const TileDesc& d);
-cudaError_t launch_tile(const TileDesc& d, int threads, cudaStream_t st);
+// One launch of the tile kernel: `nitems` CTAs, item i runs descs[items[i].desc].
+struct LaunchSpec {
+  const TileDesc* descs;
+  const WorkItem* items;
+  int nitems;
+  int threads;
+  int smem_data;      // float2 per ping-pong buffer (max over the launch's descriptors)
+  size_t smem_bytes;  // dynamic shared memory of the launch
+};
+size_t tile_smem_bytes(int smem_data, int tw_total, int G);
+cudaError_t launch_tiles(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st);
 
 // ------------------------------------------------------------- map kernel
 // Element-wise index maps and pointwise products between two views, one
@@ -33,15 +44,13 @@ struct MapDesc {
   i64 n, m, nm;        // map parameters
   const int* tab;
   const float2* vec;
-  float2* dc;          // per-line DC (Rader: sum of the permuted inputs)
-  float2* x0;          // per-line x[0] (Rader)
-  i64 dc_ws, x0_ws;    // workspace offsets of dc / x0 (host side, -1 = none)
+  i64 dc_ws, x0_ws;    // workspace offsets of the per-line DC / x0 (-1 = none)
   const float2* tab_tw;  // two-level twiddle table of n (MAP_TWIDDLE)
   int tw_log2;
   float tw_sign;
   float scale;
 };
-cudaError_t launch_map(const MapDesc& d, cudaStream_t st);
+cudaError_t launch_map(const MapDesc& d, const TileBases& bases, cudaStream_t st);
 
 // ------------------------------------------------------------- tables (FP64)
 // tab[i] = exp(-2 pi i t_i / n) for the two-level layout: t_i = i (i < S),
@@ -52,12 +61,5 @@ cudaError_t launch_twiddle_table(float2* dst, i64 n, int S, int H, cudaStream_t 
 cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cudaStream_t st);
 // Rader kernel[i] = exp(sign * 2 pi i * (g^i mod p) / p) (Planned.hs:655-659)
 cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st);
-
-// ------------------------------------------------------------- other kernels
-cudaError_t launch_karatsuba_i64(const int64_t* x, const int64_t* y, int64_t* z, i64 L, i64 batch,
-                                 int64_t* ws, cudaStream_t st);
-cudaError_t launch_karatsuba_i32(const int32_t* x, const int32_t* y, int64_t* z, i64 L, i64 batch,
-                                 int64_t* ws, cudaStream_t st);
-i64 karatsuba_ws_elems(i64 L, i64 batch);
 
 }  // namespace af

@@ -10,53 +10,54 @@ __device__ __forceinline__ i64 view_addr(const IoDesc& io, i64 line, i64 e) {
   const i64 lo_cnt = io.lo_div.d;
   const i64 hi = line / lo_cnt;
   const i64 lo = line - hi * lo_cnt;
-  return hi * io.s_hi + lo * io.s_lo + e * io.s_e;
+  return io.off + hi * io.s_hi + lo * io.s_lo + e * io.s_e;
 }
-__device__ __forceinline__ float2 vload(const IoDesc& io, i64 a) {
-  if (io.c) return io.c[a];
-  return make_float2(io.re[a], io.im[a]);
+__device__ __forceinline__ float2 vload(const TileBases& B, const IoDesc& io, i64 a) {
+  if (B.c[io.buf]) return B.c[io.buf][a];
+  return make_float2(B.re[io.buf][a], B.im[io.buf][a]);
 }
-__device__ __forceinline__ void vstore(const IoDesc& io, i64 a, float2 v) {
-  if (io.c) io.c[a] = v;
-  else { io.re[a] = v.x; io.im[a] = v.y; }
+__device__ __forceinline__ void vstore(const TileBases& B, const IoDesc& io, i64 a, float2 v) {
+  if (B.c[io.buf]) B.c[io.buf][a] = v;
+  else { B.re[io.buf][a] = v.x; B.im[io.buf][a] = v.y; }
 }
 
-__global__ void map_kernel(const MapDesc d) {
+__global__ void map_kernel(const MapDesc d, const TileBases B) {
   const i64 total = d.nlines * d.nout;
+  float2* ws = B.c[BUF_WS];
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
     const i64 line = q / d.nout;
     const i64 e = q - line * d.nout;
     float2 v;
     switch (d.mode) {
-      case MAP_COPY: v = vload(d.in, view_addr(d.in, line, e)); break;
+      case MAP_COPY: v = vload(B, d.in, view_addr(d.in, line, e)); break;
       case MAP_GT_IN: {
         const i64 k = e / d.n, j = e - k * d.n;
-        v = vload(d.in, view_addr(d.in, line, (d.n * k + d.m * j) % d.nm));
+        v = vload(B, d.in, view_addr(d.in, line, (d.n * k + d.m * j) % d.nm));
         break;
       }
       case MAP_GT_OUT:
-        v = vload(d.in, view_addr(d.in, line, (e % d.n) * d.m + (e % d.m)));
+        v = vload(B, d.in, view_addr(d.in, line, (e % d.n) * d.m + (e % d.m)));
         break;
       case MAP_TABLE:
-        v = vload(d.in, view_addr(d.in, line, d.tab[e]));
-        if (d.x0 && e == 0) d.x0[line] = vload(d.in, view_addr(d.in, line, 0));
+        v = vload(B, d.in, view_addr(d.in, line, d.tab[e]));
+        if (d.x0_ws >= 0 && e == 0) ws[d.x0_ws + line] = vload(B, d.in, view_addr(d.in, line, 0));
         break;
       case MAP_RADER_OUT: {
-        const float2 x0 = d.x0[line];
-        const float2 c = e == 0 ? d.dc[line] : vload(d.in, view_addr(d.in, line, d.tab[e - 1]));
+        const float2 x0 = ws[d.x0_ws + line];
+        const float2 c = e == 0 ? ws[d.dc_ws + line] : vload(B, d.in, view_addr(d.in, line, d.tab[e - 1]));
         v = cadd(x0, c);
         break;
       }
       case MAP_CHIRP_IN:
-        v = e < d.n ? cmul(d.vec[e], vload(d.in, view_addr(d.in, line, e))) : make_float2(0.f, 0.f);
+        v = e < d.n ? cmul(d.vec[e], vload(B, d.in, view_addr(d.in, line, e))) : make_float2(0.f, 0.f);
         break;
       case MAP_MUL: {
-        const float2 u = vload(d.in, view_addr(d.in, line, e));
-        if (d.dc && e == 0) d.dc[line] = u;
+        const float2 u = vload(B, d.in, view_addr(d.in, line, e));
+        if (d.dc_ws >= 0 && e == 0) ws[d.dc_ws + line] = u;
         v = cmul(d.vec[e], u);
         break;
       }
-      case MAP_SCALE: v = cscale(vload(d.in, view_addr(d.in, line, e)), d.scale); break;
+      case MAP_SCALE: v = cscale(vload(B, d.in, view_addr(d.in, line, e)), d.scale); break;
       case MAP_TWIDDLE: {
         const i64 col = line % d.m;
         const i64 t = (col * e) % d.n;
@@ -64,25 +65,25 @@ __global__ void map_kernel(const MapDesc d) {
         const float2 hi = d.tab_tw[(1 << d.tw_log2) + (t >> d.tw_log2)];
         float2 w = cmul(hi, lo);
         w.y *= -d.tw_sign;
-        v = cmul(vload(d.in, view_addr(d.in, line, e)), w);
+        v = cmul(vload(B, d.in, view_addr(d.in, line, e)), w);
         break;
       }
       default: {  // MAP_REVERSE
         const i64 s = e == 0 ? 0 : d.n - e;
-        v = vload(d.in, view_addr(d.in, line, s));
+        v = vload(B, d.in, view_addr(d.in, line, s));
         break;
       }
     }
-    vstore(d.out, view_addr(d.out, line, e), v);
+    vstore(B, d.out, view_addr(d.out, line, e), v);
   }
 }
 
-cudaError_t launch_map(const MapDesc& d, cudaStream_t st) {
+cudaError_t launch_map(const MapDesc& d, const TileBases& bases, cudaStream_t st) {
   const i64 total = d.nlines * d.nout;
   if (total <= 0) return cudaSuccess;
   i64 blocks = (total + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;
-  map_kernel<<<(unsigned)blocks, 256, 0, st>>>(d);
+  map_kernel<<<(unsigned)blocks, 256, 0, st>>>(d, bases);
   return cudaGetLastError();
 }
 

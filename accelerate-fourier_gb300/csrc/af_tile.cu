@@ -1,17 +1,22 @@
 // af_tile.cu -- the shared-memory tile FFT kernel of libaf.
 //
-// One CTA transforms G lines (independent transforms) held in shared memory:
-// load (through the tile kind's index map) -> one or two Stockham FFT phases
-// -> store (through the inverse map, with four-step twiddle and scale).  A
-// phase is a sequence of Stockham passes of radix 2,3,4,5,7,8,11,13 or 16
-// that alternate between two shared-memory buffers.
+// Every FFT launch of the library is this kernel: a list of work items, one
+// per CTA, each naming a tile descriptor (device memory) and the lines it
+// owns.  A CTA copies its descriptor to shared memory, loads its lines
+// through the descriptor's index map, runs one or two Stockham FFT phases
+// (passes of radix 2,3,4,5,7,8,11,13,16 alternating between two shared
+// buffers), and stores through the inverse map with the four-step twiddle,
+// scale and optional cotangent epilogue.
 //
 // Tile kinds restate the reference's algorithms (file:line relative to the
 // accelerate-fourier project):
-//   TILE_PLAIN      Cooley-Tukey / split-radix leaves (Fourier/Planned.hs:473-557)
-//   TILE_GT         Good-Thomas with the reference's CRT maps (Planned.hs:584-617)
-//   TILE_RADER      Rader's algorithm (Planned.hs:646-692, Permutation.hs:24-80)
-//   TILE_BLUESTEIN  Bluestein / chirp-z (Planned.hs:744-773, Private.hs:428-436)
+//   TILE_PLAIN      Cooley-Tukey / split-radix passes (Fourier/Planned.hs:473-557),
+//                   with Good-Thomas (584-617), Rader (646-692) and Bluestein
+//                   (760-773) index maps fused into loads and stores
+//   TILE_GT         Good-Thomas in one tile with the reference's CRT maps
+//   TILE_RADER      Rader's algorithm in one tile (Permutation.hs:24-80)
+//   TILE_BLUESTEIN  Bluestein in one tile (Private.hs:428-436)
+//   TILE_CONVROW    middle pass of a four-step cyclic convolution (Planned.hs:803-821)
 #include "af_device.cuh"
 #include "af_internal.h"
 
@@ -50,8 +55,7 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
   __syncthreads();
 }
 
-// Runs every pass of a phase staged in shared memory; returns the buffer that
-// holds the result (the two buffers alternate pass by pass).
+// Runs every pass of a phase; returns the buffer holding the result.
 template <int T>
 __device__ __noinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
                                           const float2* tab) {
@@ -78,18 +82,17 @@ __device__ __noinline__ float2* run_phase(float2* cur, float2* oth, const FftPha
   return cur;
 }
 
-__device__ __forceinline__ i64 io_addr(const IoDesc& io, int line, int e) {
-  const int hi = (int)fdiv((unsigned)line, io.lo_div);
-  const int lo = line - hi * (int)io.lo_div.d;
-  return (i64)hi * io.s_hi + (i64)lo * io.s_lo + (i64)e * io.s_e;
+__device__ __forceinline__ float2 gld(const TileBases& B, int buf, i64 a) {
+  if (B.c[buf]) return B.c[buf][a];
+  return make_float2(B.re[buf][a], B.im[buf][a]);
 }
-__device__ __forceinline__ float2 io_load(const IoDesc& io, i64 a) {
-  if (io.c) return io.c[a];
-  return make_float2(io.re[a], io.im[a]);
+__device__ __forceinline__ void gst(const TileBases& B, int buf, i64 a, float2 v) {
+  if (B.c[buf]) B.c[buf][a] = v;
+  else { B.re[buf][a] = v.x; B.im[buf][a] = v.y; }
 }
-__device__ __forceinline__ void io_store(const IoDesc& io, i64 a, float2 v) {
-  if (io.c) io.c[a] = v;
-  else { io.re[a] = v.x; io.im[a] = v.y; }
+__device__ __forceinline__ void split_line(const IoDesc& io, int line, int& hi, int& lo) {
+  hi = (int)fdiv((unsigned)line, io.lo_div);
+  lo = line - hi * (int)io.lo_div.d;
 }
 
 // Visit (line, element) pairs of G lines x N elements in the coalescing
@@ -111,29 +114,30 @@ __device__ __forceinline__ void for_tile(int G, int N, const FastDiv& Ndiv, cons
   }
 }
 
-template <int T>
-__global__ void __launch_bounds__(T) tile_kernel(const TileDesc d) {
-  extern __shared__ float2 smem[];
-  const int line0 = blockIdx.x * d.G;
-  const int G = min(d.G, d.nlines - line0);
-  if (G <= 0) return;
-  // shared layout: [A: spad(G*LS)] [B: spad(G*LS)] [tables] [scratch 2G] [phase descriptors]
-  const int dlen = spad(d.G * d.LS);
-  float2* A = smem;
-  float2* B = smem + dlen;
-  float2* tab = B + dlen;
-  float2* xs = tab + d.tw_total;
-  FftPhase* phs = reinterpret_cast<FftPhase*>(xs + 2 * d.G);
-  for (int i = threadIdx.x; i < d.tw_total; i += T) tab[i] = d.tw_src[i];
-  {
-    const int words = (int)(sizeof(FftPhase) * AF_MAXPH / 4);
-    const int* srcw = reinterpret_cast<const int*>(&d.ph[0]);
-    int* dstw = reinterpret_cast<int*>(phs);
-    for (int i = threadIdx.x; i < words; i += T) dstw[i] = srcw[i];
-  }
+struct StoreCtx {
+  const TileBases* B;
+  float loss;
+  int cot;
+};
 
+// final store of one element; the cotangent epilogue stores g = 2 w v with
+// w at the same address in BUF_AUX (real weights, interleaved as (w, 0)
+// pairs or a planar re plane) and adds w |v|^2 to the loss
+__device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, float2 v) {
+  if (sc.cot) {
+    const float w = sc.B->c[BUF_AUX] ? reinterpret_cast<const float*>(sc.B->c[BUF_AUX])[a] : sc.B->re[BUF_AUX][a];
+    sc.loss += w * (v.x * v.x + v.y * v.y);
+    v = cscale(v, 2.f * w);
+  }
+  gst(*sc.B, buf, a, v);
+}
+
+template <int T>
+__device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it, const TileBases& B,
+                                          float2* A, float2* Bf, float2* tab, float2* xs, double* loss) {
+  const int line0 = it.line0;
+  const int G = it.G;
   const int N = d.nlen;
-  // a partial last CTA walks its G lines with a divider computed here
   FastDiv Gdiv = d.G_div;
   if (G != d.G) {
     Gdiv.d = G;
@@ -143,26 +147,57 @@ __global__ void __launch_bounds__(T) tile_kernel(const TileDesc d) {
     Gdiv.m = G <= 1 ? 0u : (unsigned)(((1ull << 32) * ((1ull << s) - (unsigned)G)) / (unsigned)G + 1);
   }
   float2* sm = A;
+  const IoDesc& in = d.in;
+  const IoDesc& out = d.out;
+  const i64 ibase = in.off + it.in_add;
+  const i64 obase = out.off + it.out_add;
 
   // ------------------------------------------------------------ load
-  if (d.kind == TILE_PLAIN) {
-    for_tile<T>(G, N, d.N_div, Gdiv, d.in.line_fast, [&](int l, int e) {
-      sm[spad(l * d.LS + e)] = io_load(d.in, io_addr(d.in, line0 + l, e));
+  if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
+    for_tile<T>(G, N, d.N_div, Gdiv, in.line_fast, [&](int l, int e) {
+      int hi, lo;
+      split_line(in, line0 + l, hi, lo);
+      float2 v;
+      if (in.map == IO_AFFINE) {
+        v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e);
+      } else if (in.map == IO_GT) {
+        const i64 idx = (in.mA * lo + in.mB * e) % in.mN;
+        v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + idx * in.s_t);
+      } else if (in.map == IO_TABLE) {  // zero beyond the table length mN
+        const i64 q = lo * in.q_lo + e * in.q_e;
+        v = make_float2(0.f, 0.f);
+        if (q < in.mN) v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)__ldg(&in.tab[q]) * in.s_t);
+      } else {  // IO_CHIRP: zero pad beyond the logical length
+        const i64 q = lo * in.q_lo + e * in.q_e;
+        v = make_float2(0.f, 0.f);
+        if (q < in.mN) v = cmul(__ldg(&in.vec[q]), gld(B, in.buf, ibase + (i64)hi * in.s_hi + q * in.s_t));
+      }
+      sm[spad(l * d.LS + e)] = v;
     });
   } else if (d.kind == TILE_GT) {
     // grid position (k, j) holds x[(n k + m j) mod N]  (Planned.hs:597-606);
     // inverting: k = i*cm mod m, j = i*cn mod n
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i) {
+      int hi, lo;
+      split_line(in, line0 + l, hi, lo);
       const int k = (int)(((i64)i * d.gt_cm) % d.gt_m);
       const int j = (int)(((i64)i * d.gt_cn) % d.gt_n);
-      sm[spad(l * d.LS + k * d.gt_n + j)] = io_load(d.in, io_addr(d.in, line0 + l, i));
+      sm[spad(l * d.LS + k * d.gt_n + j)] =
+          gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)i * in.s_e);
     });
   } else if (d.kind == TILE_RADER) {
     // a[q] = x[g^-q]  (Permutation.apply rev res, Planned.hs:686-692): input
     // index r >= 1 with g^dlog(r) = r goes to q = (-dlog r) mod (p-1)
     const int m = N - 1;
+    // a convolution carried by longer transforms (slen > p-1) is zero padded
+    for (int q = threadIdx.x; q < G * (d.slen - m); q += T) {
+      const int l = q / (d.slen - m);
+      sm[spad(l * d.LS + m + (q - l * (d.slen - m)))] = make_float2(0.f, 0.f);
+    }
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
-      const float2 v = io_load(d.in, io_addr(d.in, line0 + l, r));
+      int hi, lo;
+      split_line(in, line0 + l, hi, lo);
+      const float2 v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)r * in.s_e);
       if (r == 0) {
         xs[2 * l] = v;
       } else {
@@ -173,93 +208,179 @@ __global__ void __launch_bounds__(T) tile_kernel(const TileDesc d) {
   } else {  // TILE_BLUESTEIN: chirp * x zero padded to M (Planned.hs:765-773)
     const int M = d.slen;
     for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
+      int hi, lo;
+      split_line(in, line0 + l, hi, lo);
       float2 v = make_float2(0.f, 0.f);
-      if (e < N) v = cmul(__ldg(&d.vec_a[e]), io_load(d.in, io_addr(d.in, line0 + l, e)));
+      if (e < N)
+        v = cmul(__ldg(&d.vec_a[e]),
+                 gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e));
       sm[spad(l * d.LS + e)] = v;
     });
   }
   __syncthreads();
 
   // ------------------------------------------------------------ phases
-  sm = run_phase<T>(A, B, &phs[0], d.LS, G, tab);
-  if (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN) {
-    // conv tiles: FFT(+1) -> * spectrum -> FFT(-1), the direction order of the
-    // reference's convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
+  sm = run_phase<T>(A, Bf, &d.ph[0], d.LS, G, tab);
+  if (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN || d.kind == TILE_CONVROW) {
+    // FFT(+1) -> * spectrum -> FFT(-1): the direction order of the reference's
+    // convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
     if (d.kind == TILE_RADER) {
       for (int l = threadIdx.x; l < G; l += T) xs[2 * l + 1] = sm[spad(l * d.LS)];  // sum res
       __syncthreads();
     }
     const int M = d.slen;
-    for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
-      const int a = spad(l * d.LS + e);
-      sm[a] = cmul(__ldg(&d.vec_b[e]), sm[a]);
-    });
+    if (d.kind == TILE_CONVROW) {
+      if (d.dc_off >= 0 && threadIdx.x == 0) {
+        for (int l = 0; l < G; ++l) {
+          int hi, lo;
+          split_line(out, line0 + l, hi, lo);
+          if (lo == 0) B.c[BUF_WS][d.dc_off + it.out_add + hi] = sm[spad(l * d.LS)];
+        }
+      }
+      __syncthreads();
+      for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
+        int hi, lo;
+        split_line(out, line0 + l, hi, lo);
+        const int a = spad(l * d.LS + e);
+        sm[a] = cmul(__ldg(&d.vec_b[lo * d.sq_lo + e * d.sq_e]), sm[a]);
+      });
+    } else {
+      for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
+        const int a = spad(l * d.LS + e);
+        sm[a] = cmul(__ldg(&d.vec_b[e]), sm[a]);
+      });
+    }
     __syncthreads();
   }
-  if (d.nph > 1) sm = run_phase<T>(sm, sm == A ? B : A, &phs[1], d.LS, G, tab);
+  if (d.nph > 1) sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[1], d.LS, G, tab);
 
   // ------------------------------------------------------------ store
-  if (d.kind == TILE_PLAIN) {
-    for_tile<T>(G, N, d.N_div, Gdiv, d.out.line_fast, [&](int l, int e) {
+  StoreCtx sc{&B, 0.f, d.cot};
+  if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
+    for_tile<T>(G, N, d.N_div, Gdiv, out.line_fast, [&](int l, int e) {
+      int hi, lo;
+      split_line(out, line0 + l, hi, lo);
       float2 v = sm[spad(l * d.LS + e)];
       if (d.ptw) {
-        const int line = line0 + l;
-        const int hi = (int)fdiv((unsigned)line, d.out.lo_div);
-        const i64 col = (i64)(line - hi * (int)d.out.lo_div.d) * d.ptw_col_mul;
-        const i64 t = (col * e) % d.ptwN;
-        const float2 lo = __ldg(&d.ptw[t & ((1 << d.ptwS_log2) - 1)]);
-        const float2 hh = __ldg(&d.ptw[(1 << d.ptwS_log2) + (t >> d.ptwS_log2)]);
-        float2 w = cmul(hh, lo);
+        const i64 t = ((i64)lo * e) % d.ptwN;
+        const float2 wl = __ldg(&d.ptw[t & ((1 << d.ptwS_log2) - 1)]);
+        const float2 wh = __ldg(&d.ptw[(1 << d.ptwS_log2) + (t >> d.ptwS_log2)]);
+        float2 w = cmul(wh, wl);
         w.y *= -d.ptw_sign;
         v = cmul(v, w);
       }
-      io_store(d.out, io_addr(d.out, line0 + l, e), cscale(v, d.scale));
+      v = cscale(v, d.scale);
+      const i64 hb = obase + (i64)hi * out.s_hi;
+      if (out.map == IO_AFFINE) {
+        store_final(sc, out.buf, hb + (i64)lo * out.s_lo + (i64)e * out.s_e, v);
+      } else if (out.map == IO_GT) {
+        store_final(sc, out.buf, hb + ((out.mA * lo + out.mB * e) % out.mN) * out.s_t, v);
+      } else if (out.map == IO_CHIRP) {
+        const i64 q = lo * out.q_lo + e * out.q_e;
+        if (q < out.mN) store_final(sc, out.buf, hb + q * out.s_t, cmul(__ldg(&out.vec[q]), v));
+      } else {  // IO_RADER: c[q] -> out[g^q] = x0 + c[q]; q == 0 also out[0] = x0 + dc
+        const i64 q = lo * out.q_lo + e * out.q_e;
+        if (q >= out.mN) return;  // padding of a longer convolution
+        const float2 x0 = gld(B, out.x0_buf, out.x0_off + it.out_add + (i64)hi * out.x0_shi);
+        store_final(sc, out.buf, hb + (i64)__ldg(&out.tab[q]) * out.s_t, cadd(x0, v));
+        if (q == 0) {
+          const float2 dc = B.c[BUF_WS][out.dc_off + it.in_add + hi];
+          store_final(sc, out.buf, hb, cadd(x0, cscale(dc, d.scale)));
+        }
+      }
     });
   } else if (d.kind == TILE_GT) {
     // out[r] = C[r mod n][r mod m]  (Planned.hs:608-617); C[q][p] sits at p*n + q
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
+      int hi, lo;
+      split_line(out, line0 + l, hi, lo);
       const float2 v = sm[spad(l * d.LS + (r % d.gt_m) * d.gt_n + (r % d.gt_n))];
-      io_store(d.out, io_addr(d.out, line0 + l, r), cscale(v, d.scale));
+      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)r * out.s_e,
+                  cscale(v, d.scale));
     });
   } else if (d.kind == TILE_RADER) {
     // out[0] = x0 + sum res; out[r] = x0 + c[dlog r]  (Planned.hs:686-692)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
+      int hi, lo;
+      split_line(out, line0 + l, hi, lo);
       const float2 x0 = xs[2 * l];
       const float2 v = r == 0 ? xs[2 * l + 1] : sm[spad(l * d.LS + __ldg(&d.dlog[r - 1]))];
-      io_store(d.out, io_addr(d.out, line0 + l, r), cscale(cadd(x0, v), d.scale));
+      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)r * out.s_e,
+                  cscale(cadd(x0, v), d.scale));
     });
   } else {  // Bluestein: y = chirp * (take N c)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int e) {
+      int hi, lo;
+      split_line(out, line0 + l, hi, lo);
       const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spad(l * d.LS + e)]);
-      io_store(d.out, io_addr(d.out, line0 + l, e), cscale(v, d.scale));
+      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)e * out.s_e,
+                  cscale(v, d.scale));
     });
+  }
+
+  if (d.cot && loss) {
+    float v = sc.loss;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ float red[T / 32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < T / 32; ++w) s += red[w];
+      atomicAdd(loss, s);
+    }
   }
 }
 
-size_t tile_smem_bytes(const TileDesc& d) {
-  const int data = d.G * d.LS;
-  return (size_t)(2 * (data + (data >> 4)) + d.tw_total + 2 * d.G) * sizeof(float2) +
-         sizeof(FftPhase) * AF_MAXPH;
+template <int T>
+__global__ void __launch_bounds__(T) tile_kernel(const TileDesc* __restrict__ descs,
+                                                 const WorkItem* __restrict__ items, TileBases bases,
+                                                 double* loss, int smem_data) {
+  extern __shared__ float4 smem4[];
+  float2* smem = reinterpret_cast<float2*>(smem4);
+  const WorkItem it = items[blockIdx.x];
+  // shared layout: [descriptor] [A: smem_data] [B: smem_data] [tables] [scratch 2G]
+  TileDesc* d = reinterpret_cast<TileDesc*>(smem);
+  {
+    const int words = (int)(sizeof(TileDesc) / 4);
+    const int* srcw = reinterpret_cast<const int*>(descs + it.desc);
+    int* dstw = reinterpret_cast<int*>(d);
+    for (int i = threadIdx.x; i < words; i += T) dstw[i] = srcw[i];
+  }
+  __syncthreads();
+  const int desc_f2 = (int)((sizeof(TileDesc) + 15) / 16 * 2);
+  float2* A = smem + desc_f2;
+  float2* Bf = A + smem_data;
+  float2* tab = Bf + smem_data;
+  float2* xs = tab + d->tw_total;
+  for (int i = threadIdx.x; i < d->tw_total; i += T) tab[i] = d->tw_src[i];
+  tile_body<T>(*d, it, bases, A, Bf, tab, xs, loss);
+}
+
+size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
+  return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + 2 * G) * sizeof(float2);
 }
 
 template <int T>
-static cudaError_t launch_t(const TileDesc& d, cudaStream_t st) {
+static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const int grid = (d.nlines + d.G - 1) / d.G;
-  tile_kernel<T><<<grid, T, tile_smem_bytes(d), st>>>(d);
+  tile_kernel<T><<<L.nitems, T, L.smem_bytes, st>>>(L.descs, L.items, bases, loss, L.smem_data);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile(const TileDesc& d, int threads, cudaStream_t st) {
-  if (d.nlines <= 0) return cudaSuccess;
-  if (threads == 512) return launch_t<512>(d, st);
-  if (threads == 128) return launch_t<128>(d, st);
-  return launch_t<256>(d, st);
+cudaError_t launch_tiles(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
+  if (L.nitems <= 0) return cudaSuccess;
+  switch (L.threads) {
+    case 512: return launch_t<512>(L, bases, loss, st);
+    case 128: return launch_t<128>(L, bases, loss, st);
+    default: return launch_t<256>(L, bases, loss, st);
+  }
 }
 
 }  // namespace af

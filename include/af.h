@@ -115,6 +115,28 @@ af_status af_cyclic_reverse(af_layout layout, const float* in_re,
                             const float* in_im, float* out_re, float* out_im,
                             int64_t n, int64_t batch, af_stream stream);
 
+/* Batches of mixed lengths ------------------------------------------------
+ * `count` transforms of lengths lengths[0..count) stored back to back
+ * (transform i starts at sum_{j<i} lengths[j]).  Each transform is planned
+ * like Planned.transform (Planned.hs:103-106); all of them run in a few
+ * launches: transforms that fit one CTA share launches, larger ones run their
+ * fused multi-pass schemes grouped so that the workspace stays in L2.
+ * Interleaved Complex Float32 only.  The reference applies `transform` per
+ * array; this entry point is the batched form of that call. */
+typedef struct af_batch_s* af_batch;
+af_status af_batch_create(af_batch* batch, const int64_t* lengths, int64_t count, int sign);
+af_status af_batch_destroy(af_batch batch);
+af_status af_batch_launches(af_batch batch, int64_t* launches);
+/* out = transform of every in (sign of the batch). */
+af_status af_batch_exec(af_batch batch, const float* in, float* out, af_stream stream);
+/* grad = DFT^H cot for every transform (the VJP of af_batch_exec). */
+af_status af_batch_vjp(af_batch batch, const float* cot, float* grad, af_stream stream);
+/* Forward transform with the spectral-weight epilogue of the loss
+ * L = sum_i sum_k w_ik |X_ik|^2: writes cot = dL/dconj(X) * 2 = 2 w X and sets
+ * *loss (device double) to L.  w holds one real weight per output element. */
+af_status af_batch_forward_cotangent(af_batch batch, const float* x, const float* w, float* cot,
+                                     double* loss, af_stream stream);
+
 #ifdef __cplusplus
 }
 #endif
