@@ -519,18 +519,23 @@ static bool four_step_plan(PlanRes& res, i64 n, float sign, i64 T, i64 wst, cons
   return true;
 }
 
-// Good-Thomas in two passes (Planned.hs:584-617): pass 1 FFT_n over the CRT
-// gather x[(n k + m j) mod N] (line k, element j), stored transposed; pass 2
-// FFT_m over rows, scattered by the CRT map r = CRT(q, p).
+// Good-Thomas in two passes (Planned.hs:584-617): pass 1 transforms the
+// first factor n over the CRT gather x[(n k + m j) mod N] (line k, element j)
+// and stores transposed; pass 2 transforms the second factor m over rows and
+// scatters by the CRT map r = CRT(q, p).  Either factor may be any
+// single-tile transform (split-radix, Rader, Bluestein, Good-Thomas tile).
 static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
                              const View& outb, i64 ws_base, MultiPass* mp) {
-  const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
-  if (!tile_ok(n) || !tile_ok(m)) return false;
+  const Node* na = nd->a;
+  const Node* nb = nd->b;
+  const i64 n = na->n, m = nb->n, N = nd->n;
+  if (!single_tile_ok(na) || !single_tile_ok(nb)) return false;
   View in1 = inb;
+  in1.s_lo = 0;
   in1.lo_cnt = m;
   View w1;
   w1.buf = BUF_WS; w1.off = ws_base; w1.s_e = m; w1.s_lo = 1; w1.s_hi = wst; w1.lo_cnt = m;
-  TileStep s1 = plain_step(res, n, sign, T * m, in1, w1);
+  TileStep s1 = single_step(res, na, sign, T * m, in1, w1);
   s1.d.in.map = IO_GT;
   s1.d.in.mA = n; s1.d.in.mB = m; s1.d.in.mN = N; s1.d.in.s_t = inb.s_e;
   s1.d.in.line_fast = 0;
@@ -538,8 +543,9 @@ static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i6
   View w2;
   w2.buf = BUF_WS; w2.off = ws_base; w2.s_e = 1; w2.s_lo = m; w2.s_hi = wst; w2.lo_cnt = n;
   View out2 = outb;
+  out2.s_lo = 0;
   out2.lo_cnt = n;
-  TileStep s2 = plain_step(res, m, sign, T * n, w2, out2);
+  TileStep s2 = single_step(res, nb, sign, T * n, w2, out2);
   s2.d.out.map = IO_GT;
   s2.d.out.mA = m * mod_inverse(m, n); s2.d.out.mB = n * mod_inverse(n, m); s2.d.out.mN = N;
   s2.d.out.s_t = outb.s_e;
@@ -653,12 +659,79 @@ static bool chirp_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64
   return true;
 }
 
-// Multi-pass scheme of a node: SR chains and composites as four-step,
-// coprime nodes as two-pass Good-Thomas, primes as three-pass Rader, chirp
-// nodes as three-pass Bluestein.
+static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+                       const View& outb, i64 ws_base, MultiPass* mp);
+
+// workspace stride of a transform's multi-pass scheme
+static i64 multi_pass_len(const Node* nd) {
+  if (nd->kind == N_PRIME) return rader_conv_len(nd->n);
+  if (nd->kind == N_CHIRP) return nd->a->n;
+  return nd->n;
+}
+
+// Split-radix chains and composites over a factor with no smooth four-step
+// split (one transform, T = 1): the power-of-two part of the chain (or the
+// composite's first factor) runs as strided columns with the twiddle, and the
+// remaining node (Good-Thomas, Rader, Bluestein, ...) runs over the rows
+// with its own single-tile or multi-pass scheme, storing X[k1 + n1 k2].
+static bool peel_plan(PlanRes& res, const Node* nd, float sign, i64 T, const View& inb, const View& outb,
+                      i64 ws_base, MultiPass* mp) {
+  if (T != 1) return false;
+  const i64 n = nd->n;
+  std::vector<std::pair<i64, const Node*>> cands;
+  if (nd->kind == N_SR) {
+    const Node* c = nd;
+    i64 n1 = 1;
+    for (int k = 1; k <= 10 && c->kind == N_SR; ++k) {
+      c = c->a;
+      n1 *= 2;
+      cands.emplace_back(n1, c);
+    }
+    std::reverse(cands.begin(), cands.end());
+  } else if (nd->kind == N_COMPOSITE && tile_ok(nd->a->n)) {
+    cands.emplace_back(nd->a->n, nd->b);
+  }
+  for (auto& cd : cands) {
+    const i64 n1 = cd.first, n2 = n / n1;
+    const Node* sub = cd.second;
+    MultiPass trial;
+    View a_in = inb;
+    a_in.s_e = n2 * inb.s_e; a_in.s_lo = inb.s_e; a_in.lo_cnt = n2;
+    View w;
+    w.buf = BUF_WS; w.off = ws_base; w.s_e = n2; w.s_lo = 1; w.s_hi = n; w.lo_cnt = n2;
+    trial.steps.push_back(plain_step(res, n1, sign, n2, a_in, w, n));
+    // rows k1 of W -> out[k1 + n1 k2]
+    if (single_tile_ok(sub)) {
+      View r_in;
+      r_in.buf = BUF_WS; r_in.off = ws_base; r_in.s_e = 1; r_in.s_lo = n2; r_in.s_hi = 0; r_in.lo_cnt = n1;
+      View r_out = outb;
+      r_out.s_e = n1 * outb.s_e; r_out.s_lo = outb.s_e; r_out.s_hi = 0; r_out.lo_cnt = n1;
+      trial.steps.push_back(single_step(res, sub, sign, n1, r_in, r_out));
+      trial.ws_len = n;
+    } else {
+      View r_in;
+      r_in.buf = BUF_WS; r_in.off = ws_base; r_in.s_e = 1; r_in.s_hi = n2; r_in.s_lo = 0; r_in.lo_cnt = 1;
+      View r_out = outb;
+      r_out.s_e = n1 * outb.s_e; r_out.s_hi = outb.s_e; r_out.s_lo = 0; r_out.lo_cnt = 1;
+      MultiPass sm;
+      const i64 wst = multi_pass_len(sub);
+      if (!multi_pass(res, sub, sign, n1, wst, r_in, r_out, ws_base + n, &sm)) continue;
+      for (auto& st : sm.steps) trial.steps.push_back(st);
+      trial.ws_len = n + n1 * wst + n1 + 64;
+    }
+    *mp = trial;
+    return true;
+  }
+  return false;
+}
+
+// Multi-pass scheme of a node: smooth sizes as four-step, coprime nodes as
+// two-pass Good-Thomas, primes as three-pass Rader, chirp nodes as
+// three-pass Bluestein, other split-radix/composite nodes by peeling.
 // inb/outb: single-level views whose s_hi is the stride between transforms.
 static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
                        const View& outb, i64 ws_base, MultiPass* mp) {
+  mp->steps.clear();
   switch (nd->kind) {
     case N_COPRIME:
       if (gt_two_pass_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp)) return true;
@@ -666,15 +739,11 @@ static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst,
       return four_step_plan(res, nd->n, sign, T, wst, inb, outb, ws_base, mp);
     case N_PRIME: return rader_conv_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp);
     case N_CHIRP: return chirp_conv_plan(res, nd, sign, T, wst, inb, outb, ws_base, mp);
-    default: return four_step_plan(res, nd->n, sign, T, wst, inb, outb, ws_base, mp);
+    default:
+      if (four_step_plan(res, nd->n, sign, T, wst, inb, outb, ws_base, mp)) return true;
+      mp->steps.clear();
+      return peel_plan(res, nd, sign, T, inb, outb, ws_base, mp);
   }
-}
-
-// workspace stride of a transform's multi-pass scheme
-static i64 multi_pass_len(const Node* nd) {
-  if (nd->kind == N_PRIME) return rader_conv_len(nd->n);
-  if (nd->kind == N_CHIRP) return nd->a->n;
-  return nd->n;
 }
 
 // ============================================================ programs
@@ -1014,6 +1083,7 @@ struct BatchPlan {
   float2* ws = nullptr;
   i64 fallback = 0;      // transforms executed through their own programs
   bool cot_ok = true;    // every transform has a fused program for the cotangent epilogue
+  i64 bluestein_fallbacks = 0;  // transforms whose tree has no fused scheme (run as chirp-z)
   std::vector<std::pair<i64, Program>> fb_fwd, fb_inv;  // (index, program)
 };
 
@@ -1064,6 +1134,26 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     if (multi_pass(B->res, nd, sign, 1, multi_pass_len(nd), inb, outb, 0, &b.mp)) {
       b.mp.steps.back().d.cot = cot;
       bigs.push_back(std::move(b));
+      continue;
+    }
+    // no fused scheme for this plan tree: the DFT of length n runs as one
+    // zero-padded Bluestein convolution (chirp-z) of 13-smooth length
+    i64 pad = 2 * n - 1;
+    while (!is_13smooth(pad)) ++pad;
+    const Node* ch = B->planner.chirp(n, pad);
+    if (single_tile_ok(ch)) {
+      TileStep s = single_step(B->res, ch, sign, 1, in, out);
+      s.d.cot = cot;
+      Launch& L = single[s.threads];
+      L.type = L_TILE;
+      const int di = (int)L.descs.size();
+      L.descs.push_back(s.d);
+      append_tile(L, s, di, B->offs[i], B->offs[i]);
+      B->bluestein_fallbacks++;
+    } else if (multi_pass(B->res, ch, sign, 1, multi_pass_len(ch), inb, outb, 0, &b.mp)) {
+      b.mp.steps.back().d.cot = cot;
+      bigs.push_back(std::move(b));
+      B->bluestein_fallbacks++;
     } else {
       Program p;
       build_program(B->res, nd, sign, 1, &p);

@@ -94,6 +94,11 @@ __device__ __forceinline__ void split_line(const IoDesc& io, int line, int& hi, 
   hi = (int)fdiv((unsigned)line, io.lo_div);
   lo = line - hi * (int)io.lo_div.d;
 }
+// address of element e of a line (hi, lo) for the AFFINE and GT maps
+__device__ __forceinline__ i64 io_addr(const IoDesc& io, i64 base, int hi, int lo, int e) {
+  if (io.map == IO_GT) return base + (i64)hi * io.s_hi + ((io.mA * lo + io.mB * e) % io.mN) * io.s_t;
+  return base + (i64)hi * io.s_hi + (i64)lo * io.s_lo + (i64)e * io.s_e;
+}
 
 // Visit (line, element) pairs of G lines x N elements in the coalescing
 // order asked for (element-fast or line-fast).
@@ -182,8 +187,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(in, line0 + l, hi, lo);
       const int k = (int)(((i64)i * d.gt_cm) % d.gt_m);
       const int j = (int)(((i64)i * d.gt_cn) % d.gt_n);
-      sm[spad(l * d.LS + k * d.gt_n + j)] =
-          gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)i * in.s_e);
+      sm[spad(l * d.LS + k * d.gt_n + j)] = gld(B, in.buf, io_addr(in, ibase, hi, lo, i));
     });
   } else if (d.kind == TILE_RADER) {
     // a[q] = x[g^-q]  (Permutation.apply rev res, Planned.hs:686-692): input
@@ -197,7 +201,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      const float2 v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)r * in.s_e);
+      const float2 v = gld(B, in.buf, io_addr(in, ibase, hi, lo, r));
       if (r == 0) {
         xs[2 * l] = v;
       } else {
@@ -211,9 +215,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
       float2 v = make_float2(0.f, 0.f);
-      if (e < N)
-        v = cmul(__ldg(&d.vec_a[e]),
-                 gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e));
+      if (e < N) v = cmul(__ldg(&d.vec_a[e]), gld(B, in.buf, io_addr(in, ibase, hi, lo, e)));
       sm[spad(l * d.LS + e)] = v;
     });
   }
@@ -281,7 +283,10 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       } else {  // IO_RADER: c[q] -> out[g^q] = x0 + c[q]; q == 0 also out[0] = x0 + dc
         const i64 q = lo * out.q_lo + e * out.q_e;
         if (q >= out.mN) return;  // padding of a longer convolution
-        const float2 x0 = gld(B, out.x0_buf, out.x0_off + it.out_add + (i64)hi * out.x0_shi);
+        // x0 lives with the transform's input: user input (placed like the
+        // output) or a workspace region (placed like this step's input)
+        const i64 x0_add = out.x0_buf == in.buf ? it.in_add : it.out_add;
+        const float2 x0 = gld(B, out.x0_buf, out.x0_off + x0_add + (i64)hi * out.x0_shi);
         store_final(sc, out.buf, hb + (i64)__ldg(&out.tab[q]) * out.s_t, cadd(x0, v));
         if (q == 0) {
           const float2 dc = B.c[BUF_WS][out.dc_off + it.in_add + hi];
@@ -295,8 +300,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
       const float2 v = sm[spad(l * d.LS + (r % d.gt_m) * d.gt_n + (r % d.gt_n))];
-      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)r * out.s_e,
-                  cscale(v, d.scale));
+      store_final(sc, out.buf, io_addr(out, obase, hi, lo, r), cscale(v, d.scale));
     });
   } else if (d.kind == TILE_RADER) {
     // out[0] = x0 + sum res; out[r] = x0 + c[dlog r]  (Planned.hs:686-692)
@@ -305,16 +309,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(out, line0 + l, hi, lo);
       const float2 x0 = xs[2 * l];
       const float2 v = r == 0 ? xs[2 * l + 1] : sm[spad(l * d.LS + __ldg(&d.dlog[r - 1]))];
-      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)r * out.s_e,
-                  cscale(cadd(x0, v), d.scale));
+      store_final(sc, out.buf, io_addr(out, obase, hi, lo, r), cscale(cadd(x0, v), d.scale));
     });
   } else {  // Bluestein: y = chirp * (take N c)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int e) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
       const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spad(l * d.LS + e)]);
-      store_final(sc, out.buf, obase + (i64)hi * out.s_hi + (i64)lo * out.s_lo + (i64)e * out.s_e,
-                  cscale(v, d.scale));
+      store_final(sc, out.buf, io_addr(out, obase, hi, lo, e), cscale(v, d.scale));
     });
   }
 
