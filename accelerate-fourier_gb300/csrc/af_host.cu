@@ -304,12 +304,19 @@ static IoDesc io_of(const View& v) {
 // threads per CTA and lines per CTA (G) for a tile with `slen` shared
 // elements per line; want_wide asks for >= 16 lines so that strided
 // (line-fast) global access moves whole 32-byte sectors
+// Every tile reserves the same allowance for twiddle tables (kMaxTw
+// entries) and per-line scratch (kMaxG lines), so that any mix of tiles in
+// one launch fits the shared memory the largest of them asked for.
+static const int kMaxTw = 512;
+static const int kMaxG = 256;
 static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, int* threads, int* G) {
-  const i64 budget = 227 * 1024 - (i64)sizeof(TileDesc) - 8 * (i64)tw_total - 512;
-  auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) + 16 * g <= budget; };
+  if (tw_total > kMaxTw) throw AfError(AF_ERR_UNSUPPORTED, "twiddle tables exceed the tile allowance");
+  const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - 8 * kMaxTw - 16 * kMaxG - 256;
+  auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) <= budget; };
   i64 g = std::max<i64>(1, 4096 / std::max<i64>(slen, 1));
   if (want_wide) g = std::max<i64>(g, 16);
   g = std::min(g, std::max<i64>(lines, 1));
+  g = std::min<i64>(g, kMaxG);
   while (g > 1 && !fits(g)) --g;
   if (!fits(g)) throw AfError(AF_ERR_UNSUPPORTED, "transform does not fit a tile");
   *G = (int)g;
@@ -831,7 +838,7 @@ cudaError_t run_program(const Program& prog, const TileBases& bases, double* los
       spec.nitems = (int)L.items.size();
       spec.threads = L.threads;
       spec.smem_data = L.smem_data;
-      spec.smem_bytes = tile_smem_bytes(L.smem_data, L.tw_max, L.g_max);
+      spec.smem_bytes = tile_smem_bytes(L.smem_data, kMaxTw, kMaxG);
       e = launch_tiles(spec, bases, loss, st);
     } else {
       e = launch_map(L.md, bases, st);
