@@ -324,7 +324,8 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     float v = sc.loss;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __shared__ float red[T / 32];
+    __syncthreads();  // the per-line scratch is free again: reuse it for the reduction
+    float* red = reinterpret_cast<float*>(xs);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -364,14 +365,27 @@ size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
   return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + 2 * G) * sizeof(float2);
 }
 
+// Raises the kernel's dynamic shared-memory limit to what the device allows
+// once per process (the opt-in limit less the kernel's static usage).
 template <int T>
 static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static int limit = -1;
+  if (limit < 0) {
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, tile_kernel<T>);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               optin - (int)fa.sharedSizeBytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return e;
+    }
+    limit = optin - (int)fa.sharedSizeBytes;
   }
+  if (L.smem_bytes > (size_t)limit) return cudaErrorInvalidValue;
   tile_kernel<T><<<L.nitems, T, L.smem_bytes, st>>>(L.descs, L.items, bases, loss, L.smem_data);
   return cudaGetLastError();
 }
