@@ -40,7 +40,8 @@ static void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw AfError(AF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-static const Node* root_for(Planner& pl, i64 n, int algo) {
+namespace af {
+const Node* plan_root(Planner& pl, i64 n, int algo) {
   auto need = [&](bool ok, const char* what) {
     if (!ok) throw AfError(AF_ERR_INVALID, std::string("size ") + std::to_string(n) + " is not " + what);
   };
@@ -69,6 +70,7 @@ static const Node* root_for(Planner& pl, i64 n, int algo) {
   }
   throw AfError(AF_ERR_INVALID, "unknown algorithm");
 }
+}  // namespace af
 
 static Program& program_for(af_plan_s* P, i64 batch, int sign) {
   auto key = std::make_pair((long long)batch, sign);
@@ -149,7 +151,7 @@ af_status af_plan_create(af_plan* plan, int64_t n, int sign, af_algo algo) {
     P->n = n;
     P->sign = sign;
     P->algo = algo;
-    P->root = root_for(P->planner, n, algo);
+    P->root = plan_root(P->planner, n, algo);
     // build the batch-1 program now so that tables are generated at plan time
     if (n > 0) program_for(P, 1, sign);
     check_cuda(cudaDeviceSynchronize(), "plan tables");
@@ -183,7 +185,7 @@ af_status af_plan_tree(int64_t n, af_algo algo, char* buf, size_t len) {
   AF_TRY
   if (!buf || n < 0) return fail(AF_ERR_INVALID, "bad argument");
   Planner pl;
-  const std::string s = Planner::describe(root_for(pl, n, algo));
+  const std::string s = Planner::describe(plan_root(pl, n, algo));
   if (s.size() + 1 > len) return fail(AF_ERR_INVALID, "buffer too small");
   memcpy(buf, s.c_str(), s.size() + 1);
   return AF_OK;

@@ -142,6 +142,9 @@ struct TileDesc {
   // TILE_CONVROW: spectrum index q = lo*sq_lo + e*sq_e; DC of line lo == 0,
   // element 0 after the first FFT goes to ws[dc_off + hi] (dc_off < 0: none)
   i64 sq_lo, sq_e, dc_off;
+  // x0 capture (first pass of a multi-pass Rader): x[hi][0] of the step's
+  // input goes to ws[x0_cap + out_add + hi] (x0_cap < 0: none)
+  i64 x0_cap;
 };
 
 // One CTA's work in a launch: lines [line0, line0 + G) of descriptor `desc`;

@@ -75,6 +75,11 @@ void PlanRes::release() {
 }
 
 void* PlanRes::dalloc(size_t bytes) {
+  if (dry) {  // address-checking mode: distinct fake device addresses, no device work
+    char* p = (char*)(uintptr_t)fake_next;
+    fake_next += (bytes + 511) / 256 * 256;
+    return p;
+  }
   void* p = nullptr;
   if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) throw AfError(AF_ERR_ALLOC, "cudaMalloc of plan table failed");
   allocs.push_back(p);
@@ -100,7 +105,7 @@ TwTable PlanRes::table(i64 n) {
   t.H = (int)((n + S - 1) / S);
   t.len = (int)S + t.H;
   t.p = (float2*)dalloc(sizeof(float2) * t.len);
-  cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, 0), "twiddle table");
+  if (!dry) cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, 0), "twiddle table");
   tables[n] = t;
   return t;
 }
@@ -112,8 +117,10 @@ const float2* PlanRes::pair_table(i64 a, i64 b, int* off_b) {
   auto it = pair_tables.find(key);
   if (it != pair_tables.end()) return it->second;
   float2* p = (float2*)dalloc(sizeof(float2) * (ta.len + tb.len));
-  cuda_check(cudaMemcpy(p, ta.p, sizeof(float2) * ta.len, cudaMemcpyDeviceToDevice), "table copy");
-  cuda_check(cudaMemcpy(p + ta.len, tb.p, sizeof(float2) * tb.len, cudaMemcpyDeviceToDevice), "table copy");
+  if (!dry) {
+    cuda_check(cudaMemcpy(p, ta.p, sizeof(float2) * ta.len, cudaMemcpyDeviceToDevice), "table copy");
+    cuda_check(cudaMemcpy(p + ta.len, tb.p, sizeof(float2) * tb.len, cudaMemcpyDeviceToDevice), "table copy");
+  }
   pair_tables[key] = p;
   return p;
 }
@@ -163,6 +170,16 @@ const RaderRes& PlanRes::rader_res(i64 p, int sign) {
   r.src = (int*)dalloc(sizeof(int) * m);
   r.inv = (int*)dalloc(sizeof(int) * m);
   r.gpow = (int*)dalloc(sizeof(int) * m);
+  host_tabs[r.dlog] = dlog;
+  host_tabs[r.src] = src;
+  host_tabs[r.inv] = inv;
+  host_tabs[r.gpow] = gpow;
+  if (dry) {
+    r.M = M;
+    r.zs = (float2*)dalloc(sizeof(float2) * M);
+    rader[key] = r;
+    return rader[key];
+  }
   cuda_check(cudaMemcpy(r.dlog, dlog.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.src, src.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.inv, inv.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
@@ -201,6 +218,12 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
   ChirpRes c;
   c.len = len;
   c.pad = pad;
+  if (dry) {
+    c.chirp = (float2*)dalloc(sizeof(float2) * len);
+    c.spec = (float2*)dalloc(sizeof(float2) * pad);
+    chirps[key] = c;
+    return chirps[key];
+  }
   double2* dc = nullptr;
   cuda_check(cudaMalloc(&dc, sizeof(double2) * pad), "chirp");
   cudaError_t e = launch_chirp(dc, pad, len, sign, pad, 0);
@@ -346,6 +369,7 @@ static TileDesc blank_desc() {
   memset(&d, 0, sizeof d);
   d.scale = 1.f;
   d.dc_off = -1;
+  d.x0_cap = -1;
   return d;
 }
 
@@ -501,7 +525,8 @@ static TileStep single_step(PlanRes& res, const Node* nd, float sign, i64 lines,
 // with per-item offsets and uses T = 1).
 struct MultiPass {
   std::vector<TileStep> steps;
-  i64 ws_len = 0;
+  i64 ws_len = 0;    // workspace stride per transform
+  i64 ws_total = 0;  // workspace elements the scheme touches from ws_base (all T transforms)
 };
 
 // Cooley-Tukey four-step (Planned.hs:525-557 for composite nodes; the
@@ -523,6 +548,7 @@ static bool four_step_plan(PlanRes& res, i64 n, float sign, i64 T, i64 wst, cons
   b_out.s_e = n1 * outb.s_e; b_out.s_lo = outb.s_e; b_out.lo_cnt = n1;
   mp->steps.push_back(plain_step(res, n2, sign, T * n1, b_in, b_out));
   mp->ws_len = n;
+  mp->ws_total = T * wst;
   return true;
 }
 
@@ -559,6 +585,7 @@ static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i6
   s2.d.out.line_fast = 0;
   mp->steps.push_back(s2);
   mp->ws_len = N;
+  mp->ws_total = T * wst;
   return true;
 }
 
@@ -601,7 +628,8 @@ static bool conv_plan(PlanRes& res, i64 M, const float2* S, i64 T, i64 wst, cons
   mp->steps.push_back(plain_step(res, n1, -1.f, T * n2, c_in, c_out));
   *a_step = &mp->steps[0];
   *o_step = &mp->steps[2];
-  mp->ws_len = M + 1;  // batch regions (T = 1) keep their DC slot at offset M
+  mp->ws_len = M;
+  mp->ws_total = T * wst + 2 * T;  // regions, then T DC slots, then T x0 slots
   return true;
 }
 
@@ -631,12 +659,14 @@ static bool rader_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64
   o->d.out.q_lo = 1; o->d.out.q_e = n2;
   o->d.out.mN = m;
   o->d.out.s_t = outb.s_e;
-  o->d.out.x0_buf = inb.buf;
-  o->d.out.x0_off = inb.off;
-  o->d.out.x0_shi = inb.s_hi;
+  // x0 = x[0] is captured by the first pass (before an in-place last pass
+  // overwrites the input) into the T slots after the DC slots
+  a->d.x0_cap = dc + T;
+  o->d.out.x0_buf = BUF_WS;
+  o->d.out.x0_off = dc + T;
+  o->d.out.x0_shi = 1;
   o->d.out.dc_off = dc;
   o->d.out.line_fast = 0;
-  mp->ws_len = M + 1;
   return true;
 }
 
@@ -662,7 +692,6 @@ static bool chirp_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64
   o->d.out.mN = N;
   o->d.out.s_t = outb.s_e;
   o->d.out.line_fast = 0;
-  mp->ws_len = M;
   return true;
 }
 
@@ -715,6 +744,7 @@ static bool peel_plan(PlanRes& res, const Node* nd, float sign, i64 T, const Vie
       r_out.s_e = n1 * outb.s_e; r_out.s_lo = outb.s_e; r_out.s_hi = 0; r_out.lo_cnt = n1;
       trial.steps.push_back(single_step(res, sub, sign, n1, r_in, r_out));
       trial.ws_len = n;
+      trial.ws_total = n;
     } else {
       View r_in;
       r_in.buf = BUF_WS; r_in.off = ws_base; r_in.s_e = 1; r_in.s_hi = n2; r_in.s_lo = 0; r_in.lo_cnt = 1;
@@ -724,7 +754,8 @@ static bool peel_plan(PlanRes& res, const Node* nd, float sign, i64 T, const Vie
       const i64 wst = multi_pass_len(sub);
       if (!multi_pass(res, sub, sign, n1, wst, r_in, r_out, ws_base + n, &sm)) continue;
       for (auto& st : sm.steps) trial.steps.push_back(st);
-      trial.ws_len = n + n1 * wst + n1 + 64;
+      trial.ws_len = n + sm.ws_total;
+      trial.ws_total = n + sm.ws_total;
     }
     *mp = trial;
     return true;
@@ -804,6 +835,10 @@ void finalize_program(PlanRes& res, Program& prog) {
     bytes += sizeof(WorkItem) * L.items.size();
   }
   if (!bytes) return;
+  if (res.dry) {
+    prog.dblob = (char*)res.dalloc(bytes);
+    return;
+  }
   std::vector<char> host(bytes, 0);
   for (Launch& L : prog.launches) {
     if (L.type != L_TILE) continue;
@@ -917,11 +952,12 @@ struct Lowering {
       MultiPass mp;
       const i64 mark = top;
       const i64 wsr = multi_pass_len(nd);
-      const i64 W = alloc(lines * wsr + lines + 64);
+      const i64 W = top;  // the scheme's workspace starts here; sized after planning
       View inb = in, outb = out;
       inb.s_hi = in.s_lo; inb.s_lo = 0; inb.lo_cnt = 1;
       outb.s_hi = out.s_lo; outb.s_lo = 0; outb.lo_cnt = 1;
       if (multi_pass(res, nd, sign, lines, wsr, inb, outb, W, &mp)) {
+        alloc(mp.ws_total + 64);
         for (auto& s : mp.steps) emit_step(s);
         top = mark;
         return;
@@ -1176,14 +1212,14 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     prog.launches.push_back(kv.second);
   }
   // multi-pass transforms: chunks by workspace size, one launch per pass index
-  std::sort(bigs.begin(), bigs.end(), [](const Big& a, const Big& b) { return a.mp.ws_len > b.mp.ws_len; });
+  std::sort(bigs.begin(), bigs.end(), [](const Big& a, const Big& b) { return a.mp.ws_total > b.mp.ws_total; });
   i64 peak = 0;
   size_t k = 0;
   while (k < bigs.size()) {
     i64 used = 0;
     size_t e = k;
-    while (e < bigs.size() && (e == k || used + bigs[e].mp.ws_len + 64 <= kChunkElems)) {
-      used += (bigs[e].mp.ws_len + 63) / 64 * 64 + 64;
+    while (e < bigs.size() && (e == k || used + bigs[e].mp.ws_total + 128 <= kChunkElems)) {
+      used += (bigs[e].mp.ws_total + 63) / 64 * 64 + 64;
       ++e;
     }
     size_t maxsteps = 0;
@@ -1196,7 +1232,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
       for (size_t j = k; j < e; ++j) {
         const Big& b = bigs[j];
         const i64 woff = wpos;
-        wpos += (b.mp.ws_len + 63) / 64 * 64 + 64;
+        wpos += (b.mp.ws_total + 63) / 64 * 64 + 64;
         if (st >= b.mp.steps.size()) continue;
         const TileStep& s = b.mp.steps[st];
         const i64 n = B->ns[b.i];
@@ -1224,8 +1260,11 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   finalize_program(B->res, prog);
 }
 
-BatchPlan* batch_create(const i64* ns, i64 count, int sign) {
+BatchPlan* batch_create(const i64* ns, i64 count, int sign) { return batch_create_mode(ns, count, sign, false); }
+
+BatchPlan* batch_create_mode(const i64* ns, i64 count, int sign, bool dry) {
   BatchPlan* B = new BatchPlan();
+  B->res.dry = dry;
   try {
     B->count = count;
     B->sign = sign;
@@ -1248,8 +1287,10 @@ BatchPlan* batch_create(const i64* ns, i64 count, int sign) {
     for (auto& f : B->fb_inv) ws = std::max(ws, f.second.ws_elems);
     B->fallback = (i64)B->fb_fwd.size();
     B->ws_elems = ws;
-    if (ws) cuda_check(cudaMalloc(&B->ws, sizeof(float2) * ws), "batch workspace");
-    cuda_check(cudaDeviceSynchronize(), "batch tables");
+    if (!dry) {
+      if (ws) cuda_check(cudaMalloc(&B->ws, sizeof(float2) * ws), "batch workspace");
+      cuda_check(cudaDeviceSynchronize(), "batch tables");
+    }
   } catch (...) {
     batch_destroy(B);
     throw;
@@ -1287,6 +1328,15 @@ cudaError_t batch_run(BatchPlan* B, bool inverse, const float2* in, float2* out,
   }
   return cudaSuccess;
 }
+
+const Program& batch_program(BatchPlan* B, int which) { return which == 0 ? B->fwd : (which == 1 ? B->inv : B->cot); }
+i64 batch_ws(BatchPlan* B) { return B->ws_elems; }
+i64 batch_total(BatchPlan* B) {
+  i64 t = 0;
+  for (i64 v : B->ns) t += v;
+  return t;
+}
+const void* batch_res(BatchPlan* B) { return &B->res; }
 
 i64 batch_launches(BatchPlan* B) {
   i64 n = (i64)B->fwd.launches.size();

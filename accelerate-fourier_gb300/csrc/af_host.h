@@ -80,6 +80,9 @@ struct ChirpRes {
 };
 
 struct PlanRes {
+  bool dry = false;                       // address-checking mode (no device)
+  unsigned long long fake_next = 1ull << 40;
+  std::map<const void*, std::vector<int>> host_tabs;  // host copies of index tables
   std::vector<void*> allocs;
   std::map<i64, TwTable> tables;
   std::map<std::pair<i64, i64>, const float2*> pair_tables;
@@ -105,7 +108,10 @@ void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Progra
 // Batched executor: many transforms of mixed lengths, concatenated.
 struct BatchPlan;
 BatchPlan* batch_create(const i64* ns, i64 count, int sign);
+BatchPlan* batch_create_mode(const i64* ns, i64 count, int sign, bool dry);
 void batch_destroy(BatchPlan* b);
+const void* batch_res(BatchPlan* B);
+const Node* plan_root(Planner& pl, i64 n, int algo);
 
 }  // namespace af
 

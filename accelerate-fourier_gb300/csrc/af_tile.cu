@@ -179,6 +179,13 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       }
       sm[spad(l * d.LS + e)] = v;
     });
+    if (d.x0_cap >= 0 && threadIdx.x == 0) {
+      for (int l = 0; l < G; ++l) {
+        int hi, lo;
+        split_line(in, line0 + l, hi, lo);
+        if (lo == 0) B.c[BUF_WS][d.x0_cap + it.out_add + hi] = gld(B, in.buf, ibase + (i64)hi * in.s_hi);
+      }
+    }
   } else if (d.kind == TILE_GT) {
     // grid position (k, j) holds x[(n k + m j) mod N]  (Planned.hs:597-606);
     // inverting: k = i*cm mod m, j = i*cn mod n

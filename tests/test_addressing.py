@@ -1,0 +1,76 @@
+"""CPU checks of every launch program's memory addressing (no GPU needed).
+
+The library builds its programs in a dry-run mode and replays every global
+load and store address of the tile and map kernels against the buffer sizes;
+every output element must be written exactly once, which also proves the
+Good-Thomas CRT maps and the Rader permutations are bijections.  These checks
+run before any program reaches a GPU.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def _lib():
+    from accelerate_fourier import _lib
+    L = _lib.load()
+    L.afx_check_plan.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p,
+                                 ctypes.c_size_t]
+    L.afx_check_plan.restype = ctypes.c_int
+    L.afx_check_batch.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+    L.afx_check_batch.restype = ctypes.c_int
+    return L, _lib.ALGO
+
+
+def check_plan(n, sign=-1, algo="auto", batch=1):
+    L, ALGO = _lib()
+    msg = ctypes.create_string_buffer(1024)
+    rc = L.afx_check_plan(n, sign, ALGO[algo], batch, msg, len(msg))
+    assert rc == 0, (n, algo, batch, msg.value.decode())
+
+
+def check_batch(sizes, sign=-1):
+    L, _ = _lib()
+    a = np.ascontiguousarray(np.asarray(sizes, dtype=np.int64))
+    msg = ctypes.create_string_buffer(1024)
+    rc = L.afx_check_batch(a.ctypes.data, len(a), sign, msg, len(msg))
+    assert rc == 0, msg.value.decode()
+
+
+# single tiles, four-step, two-pass Good-Thomas (plain and Rader factors),
+# Rader convolutions (smooth and zero-padded), Bluestein, peel schemes, the
+# generic recursive lowering
+SIZES = ([1, 2, 3, 4, 5, 7, 8, 13, 16, 17, 47, 83, 100, 257, 307, 1001, 1009, 1031, 4096, 4099, 8192,
+          12288, 12289, 13007, 15015, 16384, 16385, 19683, 20000, 26701, 30011, 49999, 65536, 65537,
+          11326, 36316, 47978, 39729, 2738, 99991, 1 << 20, 3 ** 12, 1001 * 1024]
+         + list(range(101, 140)))
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_plan_addressing(n):
+    check_plan(n, -1, "auto", 1)
+    if n <= 20000:
+        check_plan(n, 1, "auto", 3)
+
+
+@pytest.mark.parametrize("algo", ["decompose", "chirp2", "chirp235", "adhoc_auto", "adhoc_chirp2",
+                                  "adhoc_chirp235"])
+def test_algorithm_addressing(algo):
+    for n in [2, 3, 17, 100, 1009, 4099, 16385, 30011]:
+        check_plan(n, -1, algo, 2)
+
+
+def test_large_sizes_addressing():
+    for n in [1000003, 1 << 22]:
+        check_plan(n, -1, "auto", 1)
+
+
+def test_batch_addressing_mixed():
+    check_batch(SIZES)
+    check_batch([0, 64, 64, 0, 1000, 64, 65537, 65537, 3], +1)
+
+
+def test_batch_addressing_benchmark_workload():
+    import bench
+    check_batch(bench.workload_sizes())
