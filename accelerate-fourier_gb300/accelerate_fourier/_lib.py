@@ -47,6 +47,7 @@ SIGNATURES = {
     "af_batch_exec": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_vjp": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_forward_cotangent": ([PTR, PTR, PTR, PTR, PTR, PTR], INT),
+    "af_exec_c2c_noalloc": ([I64, INT, PTR, PTR, I64, PTR], INT),
 }
 
 

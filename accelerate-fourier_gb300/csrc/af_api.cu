@@ -24,6 +24,8 @@ static af_status fail(af_status code, const std::string& msg) {
   return code;
 }
 
+void af::set_last_error(const std::string& m) { g_err = m; }
+
 #define AF_TRY try {
 #define AF_CATCH                                                                          \
   }                                                                                       \

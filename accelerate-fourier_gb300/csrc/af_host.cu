@@ -80,6 +80,7 @@ void* PlanRes::dalloc(size_t bytes) {
     fake_next += (bytes + 511) / 256 * 256;
     return p;
   }
+  if (no_alloc) throw AfError(AF_ERR_UNSUPPORTED, "this transform needs device tables beyond the static arrays");
   void* p = nullptr;
   if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) throw AfError(AF_ERR_ALLOC, "cudaMalloc of plan table failed");
   allocs.push_back(p);
@@ -104,8 +105,14 @@ TwTable PlanRes::table(i64 n) {
   const i64 S = (i64)1 << t.S_log2;
   t.H = (int)((n + S - 1) / S);
   t.len = (int)S + t.H;
-  t.p = (float2*)dalloc(sizeof(float2) * t.len);
-  if (!dry) cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, 0), "twiddle table");
+  if (arena) {
+    if (arena_used + (size_t)t.len > arena_cap) throw AfError(AF_ERR_UNSUPPORTED, "twiddle tables exceed the arena");
+    t.p = arena + arena_used;
+    arena_used += (size_t)t.len;
+  } else {
+    t.p = (float2*)dalloc(sizeof(float2) * t.len);
+  }
+  if (!dry) cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, stream), "twiddle table");
   tables[n] = t;
   return t;
 }
@@ -844,6 +851,15 @@ void finalize_program(PlanRes& res, Program& prog) {
     if (L.type != L_TILE) continue;
     memcpy(host.data() + L.desc_off, L.descs.data(), sizeof(TileDesc) * L.descs.size());
     memcpy(host.data() + L.item_off, L.items.data(), sizeof(WorkItem) * L.items.size());
+  }
+  if (res.blob) {
+    // preallocated device area: an ordered copy on the caller's stream (a
+    // copy from pageable memory returns once the source has been consumed)
+    if (bytes > res.blob_cap) throw AfError(AF_ERR_UNSUPPORTED, "program exceeds the descriptor area");
+    prog.dblob = res.blob;
+    cuda_check(cudaMemcpyAsync(prog.dblob, host.data(), bytes, cudaMemcpyHostToDevice, res.stream),
+               "program upload");
+    return;
   }
   prog.dblob = (char*)res.dalloc(bytes);
   cuda_check(cudaMemcpy(prog.dblob, host.data(), bytes, cudaMemcpyHostToDevice), "program upload");

@@ -81,6 +81,12 @@ struct ChirpRes {
 
 struct PlanRes {
   bool dry = false;                       // address-checking mode (no device)
+  bool no_alloc = false;                  // any device allocation is an error
+  float2* arena = nullptr;                // when set, twiddle tables come from this
+  size_t arena_cap = 0, arena_used = 0;   // preallocated device area (no allocation)
+  char* blob = nullptr;                   // when set, programs upload here
+  size_t blob_cap = 0;
+  cudaStream_t stream = 0;                // stream for table generation and uploads
   unsigned long long fake_next = 1ull << 40;
   std::map<const void*, std::vector<int>> host_tabs;  // host copies of index tables
   std::vector<void*> allocs;
@@ -97,6 +103,7 @@ struct PlanRes {
 };
 
 bool tile_ok(i64 n);
+void set_last_error(const std::string& m);
 void finalize_program(PlanRes& res, Program& prog);
 cudaError_t run_program(const Program& prog, const TileBases& bases, double* loss, cudaStream_t st);
 TileBases make_bases(const float* in_re, const float* in_im, float* out_re, float* out_im, float2* ws,

@@ -287,15 +287,17 @@ def run_ours(args):
     ms_e2e = time_steps(e2e_step, args.steps, 2, torch)
 
     # plain path (one plan exec per transform) for the "vs plain" ratio
-    plain = PlainRunner(ns)
-    xs_ = torch.cuda.current_stream().cuda_stream
+    ms_plain = None
+    if not args.skip_plain:
+        plain = PlainRunner(ns)
+        xs_ = torch.cuda.current_stream().cuda_stream
 
-    def plain_step():
-        plain.forward(x, cot, xs_)
-        g = cot * (2.0 * w)
-        plain.vjp(g, grad, xs_)
+        def plain_step():
+            plain.forward(x, cot, xs_)
+            g = cot * (2.0 * w)
+            plain.vjp(g, grad, xs_)
 
-    ms_plain = time_steps(plain_step, 2, 1, torch)
+        ms_plain = time_steps(plain_step, 2, 1, torch)
 
     # accuracy vs the FP64 oracle on a sample of transforms
     from oracle import oracle as O
@@ -332,7 +334,7 @@ def run_ours(args):
                    "l2": "inputs (267 MB) larger than L2",
                    "bytes_credited_per_step": "32 * sum(n) (16 N per transform application)",
                    "ms_forward_cotangent": ms_fwd, "ms_vjp": ms_vjp,
-                   "plain_ms_per_step": ms_plain, "speedup_vs_plain": ms_plain / ms},
+                   "plain_ms_per_step": ms_plain, "speedup_vs_plain": (ms_plain / ms) if ms_plain else None},
         "e2e": {"value": nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(xh.nbytes + wh.nbytes), "d2h_bytes_per_step": int(xh.nbytes + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -382,6 +384,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true", help="skip the plain-path comparison (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

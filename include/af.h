@@ -137,6 +137,24 @@ af_status af_batch_vjp(af_batch batch, const float* cot, float* grad, af_stream 
 af_status af_batch_forward_cotangent(af_batch batch, const float* x, const float* w, float* cot,
                                      double* loss, af_stream stream);
 
+/* Power-of-two transform that allocates no device memory.
+ * This entry point has no counterpart in the reference.  It serves callers
+ * that cannot call cudaMalloc: code running inside someone else's memory pool
+ * or arena, work that must not touch the CUDA allocator while other work is
+ * captured or timed, and embedders that forbid allocation after start-up.
+ * It computes what af_exec_c2c computes for a power-of-two length n and
+ * interleaved data, with its scratch workspace, twiddle tables and launch
+ * descriptors in static device arrays of libaf (about 19 MiB, held by every
+ * GPU that loads the library until the process exits).
+ * Limit: n * batch <= 2^21 complex values; larger requests fail with
+ * AF_ERR_INVALID and a message naming the limit.  The first call on a device
+ * looks up the arrays' device addresses (once per device, with that device
+ * current): make it before any stream capture.  All calls share the arrays
+ * and each call overwrites them, so calls that overlap on the GPU race;
+ * calls issued to one stream are ordered. */
+af_status af_exec_c2c_noalloc(int64_t n, int sign, const float* in, float* out,
+                              int64_t batch, af_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

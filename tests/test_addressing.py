@@ -62,7 +62,7 @@ def test_algorithm_addressing(algo):
 
 
 def test_large_sizes_addressing():
-    for n in [1000003, 1 << 22]:
+    for n in [1000003, 1 << 21, 1 << 22]:
         check_plan(n, -1, "auto", 1)
 
 
