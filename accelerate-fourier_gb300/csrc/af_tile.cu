@@ -119,6 +119,46 @@ __device__ __forceinline__ void for_tile(int G, int N, const FastDiv& Ndiv, cons
   }
 }
 
+// global read through the read-only data path (no launch writes an address
+// that another CTA of the same launch reads)
+__device__ __forceinline__ float2 gldr(const TileBases& B, int buf, i64 a) {
+  if (B.c[buf]) return __ldg(&B.c[buf][a]);
+  return make_float2(__ldg(&B.re[buf][a]), __ldg(&B.im[buf][a]));
+}
+
+// Loads G lines x N elements into shared memory: `fetch(l, e, v)` issues the
+// load of element e of line l into v and returns its shared position.  Each
+// thread issues U fetches before writing any of them.
+template <int T, class F>
+__device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, const FastDiv& Gdiv, int line_fast,
+                                          F fetch, float2* sm) {
+  constexpr int U = 8;
+  const int tot = G * N;
+  for (int q0 = threadIdx.x; q0 < tot; q0 += T * U) {
+    float2 v[U];
+    int pos[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int q = q0 + u * T;
+      pos[u] = -1;
+      if (q < tot) {
+        int l, e;
+        if (!line_fast) {
+          l = (int)fdiv((unsigned)q, Ndiv);
+          e = q - l * N;
+        } else {
+          e = (int)fdiv((unsigned)q, Gdiv);
+          l = q - e * G;
+        }
+        pos[u] = fetch(l, e, v[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (pos[u] >= 0) sm[pos[u]] = v[u];
+  }
+}
+
 struct StoreCtx {
   const TileBases* B;
   float loss;
@@ -158,27 +198,27 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   const i64 obase = out.off + it.out_add;
 
   // ------------------------------------------------------------ load
+  // Loads are issued in groups of U independent read-only-path loads per
+  // thread before any shared-memory write, so that many are in flight.
   if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
-    for_tile<T>(G, N, d.N_div, Gdiv, in.line_fast, [&](int l, int e) {
+    load_tile<T>(G, N, d.N_div, Gdiv, in.line_fast, [&](int l, int e, float2& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      float2 v;
+      v = make_float2(0.f, 0.f);
       if (in.map == IO_AFFINE) {
-        v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e);
+        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e);
       } else if (in.map == IO_GT) {
         const i64 idx = (in.mA * lo + in.mB * e) % in.mN;
-        v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + idx * in.s_t);
+        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + idx * in.s_t);
       } else if (in.map == IO_TABLE) {  // zero beyond the table length mN
         const i64 q = lo * in.q_lo + e * in.q_e;
-        v = make_float2(0.f, 0.f);
-        if (q < in.mN) v = gld(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)__ldg(&in.tab[q]) * in.s_t);
+        if (q < in.mN) v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)__ldg(&in.tab[q]) * in.s_t);
       } else {  // IO_CHIRP: zero pad beyond the logical length
         const i64 q = lo * in.q_lo + e * in.q_e;
-        v = make_float2(0.f, 0.f);
-        if (q < in.mN) v = cmul(__ldg(&in.vec[q]), gld(B, in.buf, ibase + (i64)hi * in.s_hi + q * in.s_t));
+        if (q < in.mN) v = cmul(__ldg(&in.vec[q]), gldr(B, in.buf, ibase + (i64)hi * in.s_hi + q * in.s_t));
       }
-      sm[spad(l * d.LS + e)] = v;
-    });
+      return spad(l * d.LS + e);
+    }, sm);
     if (d.x0_cap >= 0 && threadIdx.x == 0) {
       for (int l = 0; l < G; ++l) {
         int hi, lo;
@@ -189,13 +229,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   } else if (d.kind == TILE_GT) {
     // grid position (k, j) holds x[(n k + m j) mod N]  (Planned.hs:597-606);
     // inverting: k = i*cm mod m, j = i*cn mod n
-    for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i) {
+    load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
       const int k = (int)(((i64)i * d.gt_cm) % d.gt_m);
       const int j = (int)(((i64)i * d.gt_cn) % d.gt_n);
-      sm[spad(l * d.LS + k * d.gt_n + j)] = gld(B, in.buf, io_addr(in, ibase, hi, lo, i));
-    });
+      v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, i));
+      return spad(l * d.LS + k * d.gt_n + j);
+    }, sm);
   } else if (d.kind == TILE_RADER) {
     // a[q] = x[g^-q]  (Permutation.apply rev res, Planned.hs:686-692): input
     // index r >= 1 with g^dlog(r) = r goes to q = (-dlog r) mod (p-1)
@@ -205,26 +246,24 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       const int l = q / (d.slen - m);
       sm[spad(l * d.LS + m + (q - l * (d.slen - m)))] = make_float2(0.f, 0.f);
     }
-    for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
+    const int xs_pos = (int)(xs - sm);  // x0 of line l goes to xs[2 l]
+    load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, float2& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      const float2 v = gld(B, in.buf, io_addr(in, ibase, hi, lo, r));
-      if (r == 0) {
-        xs[2 * l] = v;
-      } else {
-        const int lg = __ldg(&d.dlog[r - 1]);
-        sm[spad(l * d.LS + (lg == 0 ? 0 : m - lg))] = v;
-      }
-    });
+      v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, r));
+      if (r == 0) return xs_pos + 2 * l;
+      const int lg = __ldg(&d.dlog[r - 1]);
+      return spad(l * d.LS + (lg == 0 ? 0 : m - lg));
+    }, sm);
   } else {  // TILE_BLUESTEIN: chirp * x zero padded to M (Planned.hs:765-773)
     const int M = d.slen;
-    for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
+    load_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e, float2& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      float2 v = make_float2(0.f, 0.f);
-      if (e < N) v = cmul(__ldg(&d.vec_a[e]), gld(B, in.buf, io_addr(in, ibase, hi, lo, e)));
-      sm[spad(l * d.LS + e)] = v;
-    });
+      v = make_float2(0.f, 0.f);
+      if (e < N) v = cmul(__ldg(&d.vec_a[e]), gldr(B, in.buf, io_addr(in, ibase, hi, lo, e)));
+      return spad(l * d.LS + e);
+    }, sm);
   }
   __syncthreads();
 
@@ -344,7 +383,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
 }
 
 template <int T>
-__global__ void __launch_bounds__(T) tile_kernel(const TileDesc* __restrict__ descs,
+__global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const TileDesc* __restrict__ descs,
                                                  const WorkItem* __restrict__ items, TileBases bases,
                                                  double* loss, int smem_data) {
   extern __shared__ float4 smem4[];

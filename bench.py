@@ -233,7 +233,7 @@ def time_steps(fn, steps, warmup, torch):
 def run_ours(args):
     import torch
     torch.cuda.set_device(0)
-    ns = workload_sizes()
+    ns = workload_sizes(args.count)
     total = int(ns.sum())
     nbytes = 32 * total
     rng = np.random.default_rng(5)
@@ -306,7 +306,7 @@ def run_ours(args):
     ch = cot.cpu().numpy()
     offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
     errs = []
-    for i in range(0, COUNT, 128):
+    for i in range(0, len(ns), 128):
         n, o = int(ns[i]), int(offs[i])
         X = O.planned(xh[o:o + n].astype(np.complex128)[None], -1)[0]
         ref = 2 * wh[o:o + n] * X
@@ -385,6 +385,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true", help="skip the plain-path comparison (profiling runs)")
+    ap.add_argument("--count", type=int, default=COUNT, help="transforms in the workload (profiling runs use fewer)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
