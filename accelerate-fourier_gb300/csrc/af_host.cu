@@ -277,7 +277,7 @@ static bool four_step_split(i64 n, i64* n1, i64* n2) {
   if (!is_13smooth(n)) return false;
   i64 best = 0;
   double bestd = 1e30;
-  for (i64 a = 2; a <= 1024 && a * a <= n * 4; ++a) {
+  for (i64 a = 2; a <= 512 && a * a <= n * 4; ++a) {
     if (n % a) continue;
     const i64 b = n / a;
     if (!tile_ok(a) || !tile_ok(b)) continue;
@@ -343,15 +343,17 @@ static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, i
   if (tw_total > kMaxTw) throw AfError(AF_ERR_UNSUPPORTED, "twiddle tables exceed the tile allowance");
   const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - 8 * kMaxTw - 16 * kMaxG - 256;
   auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) <= budget; };
+  // about 4096 elements per CTA keeps three CTAs resident per SM; strided
+  // (line-fast) tiles take at least 4 lines, one 32-byte sector per row
   i64 g = std::max<i64>(1, 4096 / std::max<i64>(slen, 1));
-  if (want_wide) g = std::max<i64>(g, 16);
+  if (want_wide) g = std::max<i64>(g, 4);
   g = std::min(g, std::max<i64>(lines, 1));
   g = std::min<i64>(g, kMaxG);
   while (g > 1 && !fits(g)) --g;
   if (!fits(g)) throw AfError(AF_ERR_UNSUPPORTED, "transform does not fit a tile");
   *G = (int)g;
   const i64 elems = g * slen;
-  *threads = elems >= 6144 ? 512 : (elems >= 1024 ? 256 : 128);
+  *threads = elems > 8192 ? 512 : (elems >= 1024 ? 256 : 128);
 }
 
 struct TileStep {
@@ -1146,7 +1148,7 @@ struct BatchPlan {
   std::vector<std::pair<i64, Program>> fb_fwd, fb_inv;  // (index, program)
 };
 
-static const i64 kChunkElems = (i64)6 << 20;  // 48 MB of workspace per L2 chunk
+static const i64 kChunkElems = (i64)3 << 20;  // 24 MB of workspace per L2 chunk
 
 static void build_batch_program(BatchPlan* B, float sign, Program& prog,
                                 std::vector<std::pair<i64, Program>>& fallback, bool cot) {
