@@ -30,6 +30,30 @@ __device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
   return f.d <= 1 ? x : ((__umulhi(x, f.m) + x) >> f.s);
 }
 
+// (a * b) mod n for a, b < n < 2^31 without 64-bit division: rcp =
+// floor((2^64-1)/n) gives a quotient estimate at most 2 below the true one.
+struct ModN {
+  unsigned long long rcp;
+  unsigned n;
+};
+static inline ModN make_modn(unsigned long long n) {
+  ModN m;
+  m.n = (unsigned)n;
+  m.rcp = n ? (~0ull) / n : 0;
+  return m;
+}
+__device__ __forceinline__ unsigned mod_of(unsigned long long x, const ModN& M) {
+  const unsigned long long q = __umul64hi(x, M.rcp);
+  unsigned long long r = x - q * M.n;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (r >= M.n) r -= M.n;
+  return (unsigned)r;
+}
+__device__ __forceinline__ unsigned mulmod(unsigned a, unsigned b, const ModN& M) {
+  return mod_of((unsigned long long)a * b, M);
+}
+
 // ---------------------------------------------------------------- complex ops
 AF_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 AF_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -94,6 +118,7 @@ struct IoDesc {
   FastDiv lo_div;
   i64 q_lo, q_e;    // logical index q = lo*q_lo + e*q_e
   i64 mA, mB, mN;   // GT map constants / logical length for IO_CHIRP
+  ModN m_mod;       // IO_GT: reduction mod mN (constants mA, mB reduced mod mN)
   i64 s_t;          // element stride of a mapped transform
   const int* tab;
   const float2* vec;
@@ -131,9 +156,11 @@ struct TileDesc {
   int cot;           // 1: store g = 2 w v (w read from BUF_AUX at the output
                      // address) and add w |v|^2 to the loss
   i64 ptwN;
+  ModN ptw_mod;      // reduction mod ptwN
   // Good-Thomas tile grid m x n: logical input i sits at ((i*cm) mod m)*n + (i*cn) mod n
   int gt_n, gt_m;
   i64 gt_cm, gt_cn;
+  ModN gt_m_mod, gt_n_mod;
   // Rader: dlog[r-1] = log_g(r) for r = 1..p-1
   const int* dlog;
   // Bluestein chirp (N entries); conv spectrum (Rader zs / chirp spectrum / S)

@@ -404,6 +404,7 @@ static TileStep plain_step(PlanRes& res, i64 n, float sign, i64 lines, const Vie
     d.ptw = pt.p;
     d.ptwS_log2 = pt.S_log2;
     d.ptwN = ptwN;
+    d.ptw_mod = make_modn((unsigned long long)ptwN);
     d.ptw_sign = sign;
   }
   s.lines = lines;
@@ -456,6 +457,8 @@ static TileStep gt_step(PlanRes& res, const Node* nd, float sign, i64 lines, con
   d.gt_m = (int)m;
   d.gt_cm = mod_inverse(n, m);  // i = (n k + m j) mod N  =>  k = i n^-1 mod m
   d.gt_cn = mod_inverse(m, n);  //                           j = i m^-1 mod n
+  d.gt_m_mod = make_modn((unsigned long long)m);
+  d.gt_n_mod = make_modn((unsigned long long)n);
   d.in = io_of(in);
   d.out = io_of(out);
   d.in.line_fast = d.out.line_fast = 0;
@@ -580,6 +583,7 @@ static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i6
   TileStep s1 = single_step(res, na, sign, T * m, in1, w1);
   s1.d.in.map = IO_GT;
   s1.d.in.mA = n; s1.d.in.mB = m; s1.d.in.mN = N; s1.d.in.s_t = inb.s_e;
+  s1.d.in.m_mod = make_modn((unsigned long long)N);
   s1.d.in.line_fast = 0;
   mp->steps.push_back(s1);
   View w2;
@@ -589,7 +593,8 @@ static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i6
   out2.lo_cnt = n;
   TileStep s2 = single_step(res, nb, sign, T * n, w2, out2);
   s2.d.out.map = IO_GT;
-  s2.d.out.mA = m * mod_inverse(m, n); s2.d.out.mB = n * mod_inverse(n, m); s2.d.out.mN = N;
+  s2.d.out.mA = (m * mod_inverse(m, n)) % N; s2.d.out.mB = (n * mod_inverse(n, m)) % N; s2.d.out.mN = N;
+  s2.d.out.m_mod = make_modn((unsigned long long)N);
   s2.d.out.s_t = outb.s_e;
   s2.d.out.line_fast = 0;
   mp->steps.push_back(s2);

@@ -94,9 +94,15 @@ __device__ __forceinline__ void split_line(const IoDesc& io, int line, int& hi, 
   hi = (int)fdiv((unsigned)line, io.lo_div);
   lo = line - hi * (int)io.lo_div.d;
 }
+// (mA lo + mB e) mod mN with the constants reduced mod mN
+__device__ __forceinline__ unsigned gt_index(const IoDesc& io, int lo, int e) {
+  unsigned r = mulmod((unsigned)io.mA, (unsigned)lo, io.m_mod) + mulmod((unsigned)io.mB, (unsigned)e, io.m_mod);
+  if (r >= io.m_mod.n) r -= io.m_mod.n;
+  return r;
+}
 // address of element e of a line (hi, lo) for the AFFINE and GT maps
 __device__ __forceinline__ i64 io_addr(const IoDesc& io, i64 base, int hi, int lo, int e) {
-  if (io.map == IO_GT) return base + (i64)hi * io.s_hi + ((io.mA * lo + io.mB * e) % io.mN) * io.s_t;
+  if (io.map == IO_GT) return base + (i64)hi * io.s_hi + (i64)gt_index(io, lo, e) * io.s_t;
   return base + (i64)hi * io.s_hi + (i64)lo * io.s_lo + (i64)e * io.s_e;
 }
 
@@ -208,8 +214,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       if (in.map == IO_AFFINE) {
         v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e);
       } else if (in.map == IO_GT) {
-        const i64 idx = (in.mA * lo + in.mB * e) % in.mN;
-        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + idx * in.s_t);
+        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)gt_index(in, lo, e) * in.s_t);
       } else if (in.map == IO_TABLE) {  // zero beyond the table length mN
         const i64 q = lo * in.q_lo + e * in.q_e;
         if (q < in.mN) v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)__ldg(&in.tab[q]) * in.s_t);
@@ -232,8 +237,8 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      const int k = (int)(((i64)i * d.gt_cm) % d.gt_m);
-      const int j = (int)(((i64)i * d.gt_cn) % d.gt_n);
+      const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
+      const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
       v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, i));
       return spad(l * d.LS + k * d.gt_n + j);
     }, sm);
@@ -310,7 +315,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(out, line0 + l, hi, lo);
       float2 v = sm[spad(l * d.LS + e)];
       if (d.ptw) {
-        const i64 t = ((i64)lo * e) % d.ptwN;
+        const unsigned t = mulmod((unsigned)lo, (unsigned)e, d.ptw_mod);
         const float2 wl = __ldg(&d.ptw[t & ((1 << d.ptwS_log2) - 1)]);
         const float2 wh = __ldg(&d.ptw[(1 << d.ptwS_log2) + (t >> d.ptwS_log2)]);
         float2 w = cmul(wh, wl);
@@ -322,7 +327,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       if (out.map == IO_AFFINE) {
         store_final(sc, out.buf, hb + (i64)lo * out.s_lo + (i64)e * out.s_e, v);
       } else if (out.map == IO_GT) {
-        store_final(sc, out.buf, hb + ((out.mA * lo + out.mB * e) % out.mN) * out.s_t, v);
+        store_final(sc, out.buf, hb + (i64)gt_index(out, lo, e) * out.s_t, v);
       } else if (out.map == IO_CHIRP) {
         const i64 q = lo * out.q_lo + e * out.q_e;
         if (q < out.mN) store_final(sc, out.buf, hb + q * out.s_t, cmul(__ldg(&out.vec[q]), v));
@@ -345,7 +350,8 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 v = sm[spad(l * d.LS + (r % d.gt_m) * d.gt_n + (r % d.gt_n))];
+      const float2 v = sm[spad(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
+                               (int)mod_of((unsigned)r, d.gt_n_mod))];
       store_final(sc, out.buf, io_addr(out, obase, hi, lo, r), cscale(v, d.scale));
     });
   } else if (d.kind == TILE_RADER) {
