@@ -1161,8 +1161,15 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   fallback.clear();
   std::map<i64, const Node*> roots;
   // stage 0: single-tile transforms, one launch per thread class
-  std::map<int, Launch> single;
+  // single-tile launches are split by CTA size and shared-memory class, so
+  // that small transforms are not held to the occupancy of large ones
+  std::map<std::pair<int, int>, Launch> single;
   std::map<std::pair<i64, int>, int> single_desc;  // (n, threads) -> desc index
+  auto single_key = [](const TileStep& s) {
+    int c = 0;
+    while ((1 << c) < spad_host(s.d.G * s.d.LS) + 2) ++c;
+    return std::make_pair(s.threads, c);
+  };
   struct Big {
     i64 i;
     MultiPass mp;
@@ -1177,7 +1184,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
       TileStep s = single_step(B->res, nd, sign, 1, in, out);
       if (nd->n == 1) s = plain_step(B->res, 1, sign, 1, in, out);
       s.d.cot = cot;
-      Launch& L = single[s.threads];
+      Launch& L = single[single_key(s)];
       L.type = L_TILE;
       auto key = std::make_pair(n, s.threads);
       int di;
@@ -1210,7 +1217,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     if (single_tile_ok(ch)) {
       TileStep s = single_step(B->res, ch, sign, 1, in, out);
       s.d.cot = cot;
-      Launch& L = single[s.threads];
+      Launch& L = single[single_key(s)];
       L.type = L_TILE;
       const int di = (int)L.descs.size();
       L.descs.push_back(s.d);

@@ -22,35 +22,40 @@
 
 namespace af {
 
+// Scalars of one pass, held in registers: the descriptors live in shared
+// memory, which the passes write, so every field read in a loop would
+// otherwise be re-read from shared memory each iteration.
+struct PassRegs {
+  int n, nb, lines, LS, ls, es, lcnt, p, tw_stride, S_log2;
+  float sign;
+  FastDiv nb_div, p_div, lcnt_div;
+};
+
 // One Stockham pass, src -> dst (ping-pong shared buffers): each thread
 // walks butterflies g = tid, tid + T, ... holding one radix-R butterfly.
 template <int R, int T>
 __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, float2* __restrict__ dst,
-                                              const FftPhase& ph, int LS, int lines, const PassDesc& pd,
-                                              const float2* __restrict__ ptab) {
-  const int n = ph.n;
-  const int nb = n / R;
-  const int total = lines * nb;
-  const float sign = ph.sign;
+                                              const PassRegs r, const float2* __restrict__ ptab) {
+  const int total = r.lines * r.nb;
   for (int g = threadIdx.x; g < total; g += T) {
-    const int l = (int)fdiv((unsigned)g, pd.nb_div);
-    const int i = g - l * nb;
-    const int t = (int)fdiv((unsigned)l, ph.lcnt_div);
-    const int base = t * LS + (l - t * ph.lcnt) * ph.ls;
+    const int l = (int)fdiv((unsigned)g, r.nb_div);
+    const int i = g - l * r.nb;
+    const int t = (int)fdiv((unsigned)l, r.lcnt_div);
+    const int base = t * r.LS + (l - t * r.lcnt) * r.ls;
     float2 u[R];
 #pragma unroll
-    for (int j = 0; j < R; ++j) u[j] = src[spad(base + (i + j * nb) * ph.es)];
-    const int q = (int)fdiv((unsigned)i, pd.p_div);
-    const int k = i - q * pd.p;
+    for (int j = 0; j < R; ++j) u[j] = src[spad(base + (i + j * r.nb) * r.es)];
+    const int q = (int)fdiv((unsigned)i, r.p_div);
+    const int k = i - q * r.p;
     if (k > 0) {
-      const int st = k * pd.tw_stride;
+      const int st = k * r.tw_stride;
 #pragma unroll
-      for (int j = 1; j < R; ++j) u[j] = cmul(u[j], tw_lookup(ptab, ph.twS_log2, j * st, sign));
+      for (int j = 1; j < R; ++j) u[j] = cmul(u[j], tw_lookup(ptab, r.S_log2, j * st, r.sign));
     }
-    Dft<R>::run(u, sign, ptab, ph.twS_log2, n);
-    const int ob = q * pd.p * R + k;
+    Dft<R>::run(u, r.sign, ptab, r.S_log2, r.n);
+    const int ob = q * r.p * R + k;
 #pragma unroll
-    for (int j = 0; j < R; ++j) dst[spad(base + (ob + j * pd.p) * ph.es)] = u[j];
+    for (int j = 0; j < R; ++j) dst[spad(base + (ob + j * r.p) * r.es)] = u[j];
   }
   __syncthreads();
 }
@@ -59,21 +64,35 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
 template <int T>
 __device__ __noinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
                                           const float2* tab) {
-  const FftPhase& ph = *phs;
-  const int lines = G * ph.lcnt;
-  const float2* ptab = tab + ph.tw_off;
-  for (int p = 0; p < ph.npass; ++p) {
-    const PassDesc& pd = ph.pass[p];
+  PassRegs r;
+  r.n = phs->n;
+  r.lines = G * phs->lcnt;
+  r.LS = LS;
+  r.ls = phs->ls;
+  r.es = phs->es;
+  r.lcnt = phs->lcnt;
+  r.lcnt_div = phs->lcnt_div;
+  r.S_log2 = phs->twS_log2;
+  r.sign = phs->sign;
+  const float2* ptab = tab + phs->tw_off;
+  const int npass = phs->npass;
+  for (int p = 0; p < npass; ++p) {
+    const PassDesc pd = phs->pass[p];
+    r.nb = r.n / pd.R;
+    r.p = pd.p;
+    r.tw_stride = pd.tw_stride;
+    r.nb_div = pd.nb_div;
+    r.p_div = pd.p_div;
     switch (pd.R) {
-      case 2: stockham_pass<2, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 3: stockham_pass<3, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 4: stockham_pass<4, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 5: stockham_pass<5, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 7: stockham_pass<7, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 8: stockham_pass<8, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 11: stockham_pass<11, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 13: stockham_pass<13, T>(cur, oth, ph, LS, lines, pd, ptab); break;
-      case 16: stockham_pass<16, T>(cur, oth, ph, LS, lines, pd, ptab); break;
+      case 2: stockham_pass<2, T>(cur, oth, r, ptab); break;
+      case 3: stockham_pass<3, T>(cur, oth, r, ptab); break;
+      case 4: stockham_pass<4, T>(cur, oth, r, ptab); break;
+      case 5: stockham_pass<5, T>(cur, oth, r, ptab); break;
+      case 7: stockham_pass<7, T>(cur, oth, r, ptab); break;
+      case 8: stockham_pass<8, T>(cur, oth, r, ptab); break;
+      case 11: stockham_pass<11, T>(cur, oth, r, ptab); break;
+      case 13: stockham_pass<13, T>(cur, oth, r, ptab); break;
+      case 16: stockham_pass<16, T>(cur, oth, r, ptab); break;
     }
     float2* tmp = cur;
     cur = oth;
@@ -165,6 +184,53 @@ __device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, con
   }
 }
 
+// A global view (IoDesc) copied into registers with its base pointer resolved.
+struct IoRegs {
+  float2* c;
+  float* re;
+  float* im;
+  i64 s_e, s_lo, s_hi, s_t;
+  FastDiv lo_div;
+  unsigned mA, mB;
+  ModN m_mod;
+  i64 q_lo, q_e, mN;
+  const int* tab;
+  const float2* vec;
+};
+__device__ __forceinline__ IoRegs io_regs(const IoDesc& io, const TileBases& B, i64 base) {
+  IoRegs r;
+  r.c = B.c[io.buf] ? B.c[io.buf] + base : nullptr;
+  r.re = B.re[io.buf] ? B.re[io.buf] + base : nullptr;
+  r.im = B.im[io.buf] ? B.im[io.buf] + base : nullptr;
+  r.s_e = io.s_e;
+  r.s_lo = io.s_lo;
+  r.s_hi = io.s_hi;
+  r.s_t = io.s_t;
+  r.lo_div = io.lo_div;
+  r.mA = (unsigned)io.mA;
+  r.mB = (unsigned)io.mB;
+  r.m_mod = io.m_mod;
+  r.q_lo = io.q_lo;
+  r.q_e = io.q_e;
+  r.mN = io.mN;
+  r.tab = io.tab;
+  r.vec = io.vec;
+  return r;
+}
+__device__ __forceinline__ float2 rld(const IoRegs& r, i64 a) {
+  if (r.c) return __ldg(&r.c[a]);
+  return make_float2(__ldg(&r.re[a]), __ldg(&r.im[a]));
+}
+__device__ __forceinline__ void rsplit(const IoRegs& r, int line, int& hi, int& lo) {
+  hi = (int)fdiv((unsigned)line, r.lo_div);
+  lo = line - hi * (int)r.lo_div.d;
+}
+__device__ __forceinline__ unsigned rgt(const IoRegs& r, int lo, int e) {
+  unsigned v = mulmod(r.mA, (unsigned)lo, r.m_mod) + mulmod(r.mB, (unsigned)e, r.m_mod);
+  if (v >= r.m_mod.n) v -= r.m_mod.n;
+  return v;
+}
+
 struct StoreCtx {
   const TileBases* B;
   float loss;
@@ -206,24 +272,48 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   // ------------------------------------------------------------ load
   // Loads are issued in groups of U independent read-only-path loads per
   // thread before any shared-memory write, so that many are in flight.
+  const int LS = d.LS;
   if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
-    load_tile<T>(G, N, d.N_div, Gdiv, in.line_fast, [&](int l, int e, float2& v) -> int {
-      int hi, lo;
-      split_line(in, line0 + l, hi, lo);
-      v = make_float2(0.f, 0.f);
-      if (in.map == IO_AFFINE) {
-        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)lo * in.s_lo + (i64)e * in.s_e);
-      } else if (in.map == IO_GT) {
-        v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)gt_index(in, lo, e) * in.s_t);
-      } else if (in.map == IO_TABLE) {  // zero beyond the table length mN
-        const i64 q = lo * in.q_lo + e * in.q_e;
-        if (q < in.mN) v = gldr(B, in.buf, ibase + (i64)hi * in.s_hi + (i64)__ldg(&in.tab[q]) * in.s_t);
-      } else {  // IO_CHIRP: zero pad beyond the logical length
-        const i64 q = lo * in.q_lo + e * in.q_e;
-        if (q < in.mN) v = cmul(__ldg(&in.vec[q]), gldr(B, in.buf, ibase + (i64)hi * in.s_hi + q * in.s_t));
-      }
-      return spad(l * d.LS + e);
-    }, sm);
+    const IoRegs r = io_regs(in, B, ibase);
+    const int lf = in.line_fast;
+    switch (in.map) {
+      case IO_AFFINE:
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          int hi, lo;
+          rsplit(r, line0 + l, hi, lo);
+          v = rld(r, (i64)hi * r.s_hi + (i64)lo * r.s_lo + (i64)e * r.s_e);
+          return spad(l * LS + e);
+        }, sm);
+        break;
+      case IO_GT:
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          int hi, lo;
+          rsplit(r, line0 + l, hi, lo);
+          v = rld(r, (i64)hi * r.s_hi + (i64)rgt(r, lo, e) * r.s_t);
+          return spad(l * LS + e);
+        }, sm);
+        break;
+      case IO_TABLE:  // zero beyond the table length mN
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          int hi, lo;
+          rsplit(r, line0 + l, hi, lo);
+          const i64 q = lo * r.q_lo + e * r.q_e;
+          v = make_float2(0.f, 0.f);
+          if (q < r.mN) v = rld(r, (i64)hi * r.s_hi + (i64)__ldg(&r.tab[q]) * r.s_t);
+          return spad(l * LS + e);
+        }, sm);
+        break;
+      default:  // IO_CHIRP: zero pad beyond the logical length
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          int hi, lo;
+          rsplit(r, line0 + l, hi, lo);
+          const i64 q = lo * r.q_lo + e * r.q_e;
+          v = make_float2(0.f, 0.f);
+          if (q < r.mN) v = cmul(__ldg(&r.vec[q]), rld(r, (i64)hi * r.s_hi + q * r.s_t));
+          return spad(l * LS + e);
+        }, sm);
+        break;
+    }
     if (d.x0_cap >= 0 && threadIdx.x == 0) {
       for (int l = 0; l < G; ++l) {
         int hi, lo;
@@ -310,41 +400,59 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   // ------------------------------------------------------------ store
   StoreCtx sc{&B, 0.f, d.cot};
   if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
+    const IoRegs ro = io_regs(out, B, obase);
+    const float2* __restrict__ ptw = d.ptw;
+    const int ptwS = d.ptwS_log2;
+    const ModN pmod = d.ptw_mod;
+    const float psign = d.ptw_sign;
+    const float scale = d.scale;
+    const int cot = d.cot;
+    const float* __restrict__ wp = B.c[BUF_AUX] ? reinterpret_cast<const float*>(B.c[BUF_AUX]) : B.re[BUF_AUX];
+    const int omap = out.map;
+    // Rader scatter: x0 of transform hi and the DC slot
+    const float2* x0p = B.c[out.x0_buf] + out.x0_off + (out.x0_buf == in.buf ? it.in_add : it.out_add);
+    const i64 x0_shi = out.x0_shi;
+    const float2* dcp = B.c[BUF_WS] + out.dc_off + it.in_add;
+    float lsum = 0.f;
+    auto put = [&](i64 rel, float2 v) {
+      if (cot) {
+        const float w = __ldg(&wp[obase + rel]);
+        lsum += w * (v.x * v.x + v.y * v.y);
+        v = cscale(v, 2.f * w);
+      }
+      if (ro.c) ro.c[rel] = v;
+      else { ro.re[rel] = v.x; ro.im[rel] = v.y; }
+    };
     for_tile<T>(G, N, d.N_div, Gdiv, out.line_fast, [&](int l, int e) {
       int hi, lo;
-      split_line(out, line0 + l, hi, lo);
-      float2 v = sm[spad(l * d.LS + e)];
-      if (d.ptw) {
-        const unsigned t = mulmod((unsigned)lo, (unsigned)e, d.ptw_mod);
-        const float2 wl = __ldg(&d.ptw[t & ((1 << d.ptwS_log2) - 1)]);
-        const float2 wh = __ldg(&d.ptw[(1 << d.ptwS_log2) + (t >> d.ptwS_log2)]);
+      rsplit(ro, line0 + l, hi, lo);
+      float2 v = sm[spad(l * LS + e)];
+      if (ptw) {
+        const unsigned t = mulmod((unsigned)lo, (unsigned)e, pmod);
+        const float2 wl = __ldg(&ptw[t & ((1u << ptwS) - 1)]);
+        const float2 wh = __ldg(&ptw[(1u << ptwS) + (t >> ptwS)]);
         float2 w = cmul(wh, wl);
-        w.y *= -d.ptw_sign;
+        w.y *= -psign;
         v = cmul(v, w);
       }
-      v = cscale(v, d.scale);
-      const i64 hb = obase + (i64)hi * out.s_hi;
-      if (out.map == IO_AFFINE) {
-        store_final(sc, out.buf, hb + (i64)lo * out.s_lo + (i64)e * out.s_e, v);
-      } else if (out.map == IO_GT) {
-        store_final(sc, out.buf, hb + (i64)gt_index(out, lo, e) * out.s_t, v);
-      } else if (out.map == IO_CHIRP) {
-        const i64 q = lo * out.q_lo + e * out.q_e;
-        if (q < out.mN) store_final(sc, out.buf, hb + q * out.s_t, cmul(__ldg(&out.vec[q]), v));
+      v = cscale(v, scale);
+      const i64 hb = (i64)hi * ro.s_hi;
+      if (omap == IO_AFFINE) {
+        put(hb + (i64)lo * ro.s_lo + (i64)e * ro.s_e, v);
+      } else if (omap == IO_GT) {
+        put(hb + (i64)rgt(ro, lo, e) * ro.s_t, v);
+      } else if (omap == IO_CHIRP) {
+        const i64 q = lo * ro.q_lo + e * ro.q_e;
+        if (q < ro.mN) put(hb + q * ro.s_t, cmul(__ldg(&ro.vec[q]), v));
       } else {  // IO_RADER: c[q] -> out[g^q] = x0 + c[q]; q == 0 also out[0] = x0 + dc
-        const i64 q = lo * out.q_lo + e * out.q_e;
-        if (q >= out.mN) return;  // padding of a longer convolution
-        // x0 lives with the transform's input: user input (placed like the
-        // output) or a workspace region (placed like this step's input)
-        const i64 x0_add = out.x0_buf == in.buf ? it.in_add : it.out_add;
-        const float2 x0 = gld(B, out.x0_buf, out.x0_off + x0_add + (i64)hi * out.x0_shi);
-        store_final(sc, out.buf, hb + (i64)__ldg(&out.tab[q]) * out.s_t, cadd(x0, v));
-        if (q == 0) {
-          const float2 dc = B.c[BUF_WS][out.dc_off + it.in_add + hi];
-          store_final(sc, out.buf, hb, cadd(x0, cscale(dc, d.scale)));
-        }
+        const i64 q = lo * ro.q_lo + e * ro.q_e;
+        if (q >= ro.mN) return;  // padding of a longer convolution
+        const float2 x0 = x0p[(i64)hi * x0_shi];
+        put(hb + (i64)__ldg(&ro.tab[q]) * ro.s_t, cadd(x0, v));
+        if (q == 0) put(hb, cadd(x0, cscale(dcp[hi], scale)));
       }
     });
+    sc.loss = lsum;
   } else if (d.kind == TILE_GT) {
     // out[r] = C[r mod n][r mod m]  (Planned.hs:608-617); C[q][p] sits at p*n + q
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
