@@ -48,7 +48,34 @@ SIGNATURES = {
     "af_batch_vjp": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_forward_cotangent": ([PTR, PTR, PTR, PTR, PTR, PTR], INT),
     "af_exec_c2c_noalloc": ([I64, INT, PTR, PTR, I64, PTR], INT),
+    "af_cyclic_reverse_2d": ([INT, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
+    "af_exec_c2c_axis": ([PTR, INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_exec_c2c_2d": ([PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_exec_c2c_3d": ([PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_to_spectrum": ([PTR, PTR, INT, INT, PTR, PTR, I64, PTR], INT),
+    "af_from_spectrum": ([PTR, INT, PTR, PTR, PTR, I64, PTR], INT),
+    "af_vjp_to_spectrum": ([PTR, INT, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_to_spectrum": ([PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_to_spectrum_2d": ([PTR, PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_from_spectrum": ([PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_from_spectrum_2d": ([PTR, PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_untangle_spectra": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_untangle_spectra_2d": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
+    "af_entangle_spectra": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_convolve_cyclic": ([PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_karatsuba_i64": ([PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_karatsuba_i32_i64": ([PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_karatsuba_f32": ([PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_karatsuba_f64": ([PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_cyclic_fold_i64": ([PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_cyclic_fold_f32": ([PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_cyclic_fold_f64": ([PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_complex_i64": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_complex_f32": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_conv_complex_f64": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
 }
+
+FULL, HALF = 0, 1  # af_spectrum
 
 
 class AfError(RuntimeError):

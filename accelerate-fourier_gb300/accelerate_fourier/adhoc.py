@@ -47,3 +47,23 @@ def transformChirp235(sign: int, x):
 
 def plan_tree(n: int, algo: str = "adhoc_auto") -> str:
     return _lib.plan_tree(n, algo)
+
+
+def _shape_of(x):
+    return (x[0] if isinstance(x, tuple) else x).shape
+
+
+def transform2d(sign: int, x, algo: str = "adhoc_auto"):
+    """Adhoc.transform2d (Adhoc.hs:365-371) with SubTransform = Adhoc.transform
+    sign: the same algorithm over both axes, lengths read from the array."""
+    from .planned import TransformND
+    s = _shape_of(x)
+    return TransformND(Transform(check(sign), s[-1], algo), Transform(sign, s[-2], algo))(x)
+
+
+def transform3d(sign: int, x, algo: str = "adhoc_auto"):
+    """Adhoc.transform3d (Adhoc.hs:373-380)."""
+    from .planned import TransformND
+    s = _shape_of(x)
+    return TransformND(Transform(check(sign), s[-1], algo), Transform(sign, s[-2], algo),
+                       Transform(sign, s[-3], algo))(x)

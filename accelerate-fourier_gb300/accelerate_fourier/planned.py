@@ -66,3 +66,97 @@ def plan(length: int) -> str:
 
 def planDecompose(length: int) -> str:
     return _lib.plan_tree(length, "decompose")
+
+
+class TransformND:
+    """A 2-D or 3-D transform over the last axes: transforms[0] runs along
+    the last (least significant) axis, as in the reference's
+    SubTransformPair/SubTransformTriple (Preprocessed.hs:136-160); each
+    transform keeps its own sign.  libaf addresses the strided axes directly
+    instead of transposing (Adhoc.hs:365-380)."""
+
+    def __init__(self, *transforms: Transform):
+        if len(transforms) not in (2, 3):
+            raise ValueError("TransformND takes two or three transforms")
+        self.transforms = transforms
+
+    def shape_check(self, shape):
+        d = len(self.transforms)
+        if len(shape) < d:
+            raise ValueError(f"array needs at least {d} axes")
+        for k, t in enumerate(self.transforms):
+            if int(shape[-1 - k]) != t.length:
+                raise ValueError(f"axis {-1 - k} has length {shape[-1 - k]}, transform length {t.length}")
+        img = 1
+        for t in self.transforms:
+            img *= t.length
+        batch = 1
+        for s in shape[:-d]:
+            batch *= int(s)
+        return (*[t.plan for t in self.transforms], batch)
+
+    def __call__(self, x, out=None):
+        import torch
+        lib = _lib.load()
+        d = len(self.transforms)
+        if isinstance(x, tuple):
+            re, im = (t.contiguous().to(torch.float32) for t in x)
+            _tensor.require_cuda(re)
+            *plans, batch = self.shape_check(re.shape)
+            ore = torch.empty_like(re) if out is None else out[0]
+            oim = torch.empty_like(im) if out is None else out[1]
+            args = (_lib.PLANAR, re.data_ptr(), im.data_ptr(), ore.data_ptr(), oim.data_ptr(), batch,
+                    _tensor.stream_ptr())
+            res = (ore, oim)
+            n = re.numel()
+        else:
+            x = _tensor.as_c64(x)
+            *plans, batch = self.shape_check(x.shape)
+            y = torch.empty_like(x) if out is None else out
+            args = (_lib.INTERLEAVED, x.data_ptr(), None, y.data_ptr(), None, batch, _tensor.stream_ptr())
+            res = y
+            n = x.numel()
+        if n:
+            handles = [p.handle for p in plans]
+            f = lib.af_exec_c2c_2d if d == 2 else lib.af_exec_c2c_3d
+            _lib.check(f(*handles, *args))
+        return res
+
+
+def convolveCyclic(length: int):
+    """Planned.convolveCyclic (Planned.hs:779-790): a function of two complex
+    arrays of the given length, F(G(x)/n * G(y)) with the planned transforms."""
+    t = Transform(forward, length, "auto")
+
+    def conv(x, y):
+        import torch
+        if isinstance(x, tuple) != isinstance(y, tuple):
+            raise ValueError("x and y must have one layout")
+        if isinstance(x, tuple):
+            xr, xi, yr, yi = (a.contiguous().to(torch.float32) for a in (*x, *y))
+            _tensor.require_cuda(xr)
+            if xr.shape != yr.shape:
+                raise ValueError("signals must have equal size")
+            n, batch = _tensor.rows(xr)
+            if n != length:
+                raise ValueError("length mismatch")
+            ore, oim = torch.empty_like(xr), torch.empty_like(xi)
+            if xr.numel():
+                _lib.check(_lib.load().af_convolve_cyclic(t.plan.handle, _lib.PLANAR, xr.data_ptr(), xi.data_ptr(),
+                                                          yr.data_ptr(), yi.data_ptr(), ore.data_ptr(),
+                                                          oim.data_ptr(), batch, _tensor.stream_ptr()))
+            return ore, oim
+        x, y = _tensor.as_c64(x), _tensor.as_c64(y)
+        if x.shape != y.shape:
+            raise ValueError("signals must have equal size")
+        n, batch = _tensor.rows(x)
+        if n != length:
+            raise ValueError("length mismatch")
+        out = torch.empty_like(x)
+        if x.numel():
+            _lib.check(_lib.load().af_convolve_cyclic(t.plan.handle, _lib.INTERLEAVED, x.data_ptr(), None,
+                                                      y.data_ptr(), None, out.data_ptr(), None, batch,
+                                                      _tensor.stream_ptr()))
+        return out
+
+    return conv

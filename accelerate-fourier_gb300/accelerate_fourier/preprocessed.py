@@ -21,3 +21,16 @@ def dit2(sign: int, length: int) -> Transform:
 def dif2(sign: int, length: int) -> Transform:
     """Preprocessed.dif2 (Preprocessed.hs:497-515); length a power of two."""
     return Transform(sign, length, "prep_dif2")
+
+
+def transform2d(transform0: Transform, transform1: Transform):
+    """Preprocessed.transform2d (Preprocessed.hs:136-149): transform0 along the
+    last axis, transform1 along the second-to-last."""
+    from .planned import TransformND
+    return TransformND(transform0, transform1)
+
+
+def transform3d(transform0: Transform, transform1: Transform, transform2: Transform):
+    """Preprocessed.transform3d (Preprocessed.hs:151-160)."""
+    from .planned import TransformND
+    return TransformND(transform0, transform1, transform2)

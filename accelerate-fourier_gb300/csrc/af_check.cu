@@ -240,6 +240,41 @@ int afx_check_plan(int64_t n, int sign, int algo, int64_t batch, char* msg, size
   }
 }
 
+// The same for a transform along the middle axis of (outer, n, inner) arrays
+// (the programs behind af_exec_c2c_axis and the 2-D/3-D transforms).
+int afx_check_axis(int64_t n, int sign, int algo, int64_t outer, int64_t inner, char* msg, size_t len) {
+  try {
+    af_plan_s P;
+    P.res.dry = true;
+    P.n = n;
+    P.sign = sign;
+    P.root = plan_root(P.planner, n, algo);
+    View in;
+    in.buf = BUF_IN;
+    in.s_e = inner;
+    in.s_lo = 1;
+    in.lo_cnt = inner;
+    in.s_hi = n * inner;
+    View out = in;
+    out.buf = BUF_OUT;
+    Program prog;
+    build_program_view(P.res, P.root, (float)sign, outer * inner, in, out, &prog);
+    Checker c(P.res);
+    c.where = "axis program";
+    const i64 total = outer * n * inner;
+    c.sz[BUF_IN] = c.sz[BUF_OUT] = c.sz[BUF_AUX] = total;
+    c.sz[BUF_WS] = prog.ws_elems;
+    c.outw.assign((size_t)total, 0);
+    c.program(prog);
+    c.expect_out_once(total);
+    if (!c.ok()) return report(c.err, msg, len);
+    return 0;
+  } catch (const std::exception& e) {
+    report(e.what(), msg, len);
+    return -1;
+  }
+}
+
 // The same for a batch of mixed lengths (forward, VJP and cotangent programs).
 int afx_check_batch(const int64_t* ns, int64_t count, int sign, char* msg, size_t len) {
   BatchPlan* B = nullptr;

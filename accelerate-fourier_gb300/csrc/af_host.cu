@@ -112,7 +112,12 @@ TwTable PlanRes::table(i64 n) {
   } else {
     t.p = (float2*)dalloc(sizeof(float2) * t.len);
   }
-  if (!dry) cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, stream), "twiddle table");
+  if (!dry) {
+    cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, stream), "twiddle table");
+    // tables made on first use (a new length inside a call) must be complete
+    // before work on any other stream reads them
+    if (!arena) cuda_check(cudaStreamSynchronize(stream), "twiddle table");
+  }
   tables[n] = t;
   return t;
 }
@@ -1128,6 +1133,15 @@ void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Progra
   View in = View::rows(BUF_IN, 0, root->n, batch);
   View out = View::rows(BUF_OUT, 0, root->n, batch);
   L.node(root, sign, batch, in, out);
+  prog->ws_elems = L.peak;
+  finalize_program(res, *prog);
+}
+
+void build_program_view(PlanRes& res, const Node* root, float sign, i64 lines, const View& in, const View& out,
+                        Program* prog) {
+  Lowering L{res, prog};
+  prog->launches.clear();
+  L.node(root, sign, lines, in, out);
   prog->ws_elems = L.peak;
   finalize_program(res, *prog);
 }

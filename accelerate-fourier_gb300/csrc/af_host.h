@@ -111,6 +111,9 @@ TileBases make_bases(const float* in_re, const float* in_im, float* out_re, floa
 
 // Builds the launch program of one plan tree over `batch` contiguous rows.
 void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Program* prog);
+// The same over `lines` lines addressed through two-level views (strided axes).
+void build_program_view(PlanRes& res, const Node* root, float sign, i64 lines, const View& in, const View& out,
+                        Program* prog);
 
 // Batched executor: many transforms of mixed lengths, concatenated.
 struct BatchPlan;
@@ -130,7 +133,10 @@ struct af_plan_s {
   const af::Node* root = nullptr;
   af::PlanRes res;
   std::map<std::pair<long long, int>, af::Program> progs;  // (batch, sign)
+  std::map<std::tuple<long long, long long, int>, af::Program> axis_progs;  // (outer, inner, sign)
   float2* ws = nullptr;
   size_t ws_elems = 0;
+  float2* stage = nullptr;  // staging for the real transforms and convolutions
+  size_t stage_elems = 0;
   ~af_plan_s();
 };

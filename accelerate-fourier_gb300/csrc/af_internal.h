@@ -62,4 +62,20 @@ cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cu
 // Rader kernel[i] = exp(sign * 2 pi i * (g^i mod p) / p) (Planned.hs:655-659)
 cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st);
 
+// ------------------------------------------------------------- real / two-real / convolution maps
+// A complex array: interleaved when c is set, else planar re/im.
+struct CPtr {
+  float2* c;
+  float* re;
+  float* im;
+};
+cudaError_t launch_real_untangle(const float2* Z, CPtr out, i64 n2, i64 nout, i64 rows, const float2* tab,
+                                 int S_log2, cudaStream_t st);
+cudaError_t launch_real_entangle(CPtr spec, float2* f, i64 n2, i64 rows, const float2* tab, int S_log2, int herm,
+                                 cudaStream_t st);
+cudaError_t launch_untangle(CPtr S, CPtr A, CPtr B, i64 h, i64 w, i64 total, cudaStream_t st);
+cudaError_t launch_reverse2d(CPtr in, CPtr out, i64 h, i64 w, i64 total, cudaStream_t st);
+cudaError_t launch_entangle(CPtr C, CPtr D, CPtr out, i64 total, cudaStream_t st);
+cudaError_t launch_conv_mul(float2* gx, const float2* gy, float s, i64 total, cudaStream_t st);
+
 }  // namespace af

@@ -115,6 +115,13 @@ af_status af_cyclic_reverse(af_layout layout, const float* in_re,
                             const float* in_im, float* out_re, float* out_im,
                             int64_t n, int64_t batch, af_stream stream);
 
+/* Cyclic.reverse2d (Cyclic.hs:30-39): out[y,x] = in[-y mod height,
+ * -x mod width] for (batch, height, width) arrays; no overlap. */
+af_status af_cyclic_reverse_2d(af_layout layout, const float* in_re,
+                               const float* in_im, float* out_re, float* out_im,
+                               int64_t height, int64_t width, int64_t batch,
+                               af_stream stream);
+
 /* Batches of mixed lengths ------------------------------------------------
  * `count` transforms of lengths lengths[0..count) stored back to back
  * (transform i starts at sum_{j<i} lengths[j]).  Each transform is planned
@@ -136,6 +143,138 @@ af_status af_batch_vjp(af_batch batch, const float* cot, float* grad, af_stream 
  * *loss (device double) to L.  w holds one real weight per output element. */
 af_status af_batch_forward_cotangent(af_batch batch, const float* x, const float* w, float* cot,
                                      double* loss, af_stream stream);
+
+/* Multi-axis transforms -----------------------------------------------------
+ * Along one axis of an (outer, n, inner) row-major array, n = plan's length,
+ * with the plan's sign; inner = 1 is af_exec_c2c.  The reference transposes
+ * (LinearAlgebra.transpose, Fourier/Private.hs:414-425 cycleDim3) around a
+ * last-axis transform; here the kernels address the strided axis directly. */
+af_status af_exec_c2c_axis(af_plan plan, af_layout layout, const float* in_re,
+                           const float* in_im, float* out_re, float* out_im,
+                           int64_t outer, int64_t inner, af_stream stream);
+/* Adhoc.transform2d / Preprocessed.transform2d (Adhoc.hs:365-371,
+ * Preprocessed.hs:142-149): an array (batch, n1, n0) with n0 = plan0's
+ * length (last axis, the reference's least-significant `transform0`) and
+ * n1 = plan1's length.  Each plan applies its own sign.  in == out allowed. */
+af_status af_exec_c2c_2d(af_plan plan0, af_plan plan1, af_layout layout,
+                         const float* in_re, const float* in_im, float* out_re,
+                         float* out_im, int64_t batch, af_stream stream);
+/* Adhoc.transform3d / Preprocessed.transform3d (Adhoc.hs:373-380,
+ * Preprocessed.hs:151-160): (batch, n2, n1, n0), plan0 on the last axis. */
+af_status af_exec_c2c_3d(af_plan plan0, af_plan plan1, af_plan plan2,
+                         af_layout layout, const float* in_re,
+                         const float* in_im, float* out_re, float* out_im,
+                         int64_t batch, af_stream stream);
+
+/* Real transforms (Real.hs) ------------------------------------------------
+ * `half` is the plan of the half-length complex transform the reference takes
+ * as its `subTrans` argument: length N/2 for real rows of even length N. */
+typedef enum {
+  AF_SPECTRUM_FULL = 0, /* all N bins, as Real.toSpectrum returns them   */
+  AF_SPECTRUM_HALF = 1  /* bins 0..N/2 (N/2+1 values), the rest is their
+                           conjugate mirror; no reference counterpart   */
+} af_spectrum;
+/* Real.toSpectrum (Real.hs:49-70): x is batch x N reals (8-byte aligned),
+ * out is batch x N (FULL) or batch x (N/2+1) (HALF) complex values. */
+af_status af_to_spectrum(af_plan half, const float* x, af_spectrum spectrum,
+                         af_layout layout, float* out_re, float* out_im,
+                         int64_t batch, af_stream stream);
+/* Real.fromSpectrum (Real.hs:92-108): a self-adjoint spectrum of N bins per
+ * row -> N reals, unscaled; `half` is normally an inverse plan of N/2. */
+af_status af_from_spectrum(af_plan half, af_layout layout, const float* spec_re,
+                           const float* spec_im, float* x, int64_t batch,
+                           af_stream stream);
+/* Adjoint (VJP) of af_to_spectrum (FULL) with a forward `half` plan:
+ * grad = Re(DFT_N^H cot) for a cotangent of N complex values per row, through
+ * the half-length inverse transform.  The reference has no AD. */
+af_status af_vjp_to_spectrum(af_plan half, af_layout layout, const float* cot_re,
+                             const float* cot_im, float* grad, int64_t batch,
+                             af_stream stream);
+
+/* Two real signals through one complex transform (Real.hs:129-240).
+ * twoToSpectrum: f, g are batch x n reals (the pair array's two components);
+ * a, b receive their spectra.  The 2-D forms use af_exec_c2c_2d's shapes. */
+af_status af_two_to_spectrum(af_plan plan, const float* f, const float* g,
+                             af_layout layout, float* a_re, float* a_im,
+                             float* b_re, float* b_im, int64_t batch,
+                             af_stream stream);
+af_status af_two_to_spectrum_2d(af_plan plan0, af_plan plan1, const float* f,
+                                const float* g, af_layout layout, float* a_re,
+                                float* a_im, float* b_re, float* b_im,
+                                int64_t batch, af_stream stream);
+/* twoFromSpectrum: entangle the two spectra, transform, and split the result
+ * into its real (f) and imaginary (g) parts. */
+af_status af_two_from_spectrum(af_plan plan, af_layout layout, const float* a_re,
+                               const float* a_im, const float* b_re,
+                               const float* b_im, float* f, float* g,
+                               int64_t batch, af_stream stream);
+af_status af_two_from_spectrum_2d(af_plan plan0, af_plan plan1, af_layout layout,
+                                  const float* a_re, const float* a_im,
+                                  const float* b_re, const float* b_im, float* f,
+                                  float* g, int64_t batch, af_stream stream);
+/* untangleSpectra (Real.hs:168-172): a = (s + conj(rev s))/2,
+ * b = (s - conj(rev s))(-i/2).  s must not overlap a or b. */
+af_status af_untangle_spectra(af_layout layout, const float* s_re,
+                              const float* s_im, float* a_re, float* a_im,
+                              float* b_re, float* b_im, int64_t n,
+                              int64_t batch, af_stream stream);
+/* untangleSpectra2d (Real.hs:174-179): the reverse runs over both axes of
+ * (batch, height, width). */
+af_status af_untangle_spectra_2d(af_layout layout, const float* s_re,
+                                 const float* s_im, float* a_re, float* a_im,
+                                 float* b_re, float* b_im, int64_t height,
+                                 int64_t width, int64_t batch, af_stream stream);
+/* entangleSpectra(2d) (Real.hs:207-236): out = c + i d, element-wise. */
+af_status af_entangle_spectra(af_layout layout, const float* c_re,
+                              const float* c_im, const float* d_re,
+                              const float* d_im, float* out_re, float* out_im,
+                              int64_t n, int64_t batch, af_stream stream);
+
+/* Convolutions -------------------------------------------------------------
+ * Planned.convolveCyclic (Planned.hs:779-821): out = F(G(x)/n * G(y)) with
+ * G the inverse (+1) and F the forward (-1) transform of the plan's length
+ * and algorithm (the plan's own sign is not used).  n must be non-zero. */
+af_status af_convolve_cyclic(af_plan plan, af_layout layout, const float* x_re,
+                             const float* x_im, const float* y_re,
+                             const float* y_im, float* out_re, float* out_im,
+                             int64_t batch, af_stream stream);
+/* Convolution.Adhoc.karatsuba (Convolution/Adhoc.hs:36-98): linear
+ * convolution of batch rows of length L into batch rows of 2L-1 (none for
+ * L = 0).  Integer results are exact (two's-complement wrap-around, like the
+ * reference's Int arithmetic); the i32 form widens its inputs to int64.
+ * Floating-point results follow the reference's order of operations.
+ * Scratch comes from the stream-ordered allocator (cudaMallocAsync). */
+af_status af_karatsuba_i64(const int64_t* x, const int64_t* y, int64_t* z,
+                           int64_t L, int64_t batch, af_stream stream);
+af_status af_karatsuba_i32_i64(const int32_t* x, const int32_t* y, int64_t* z,
+                               int64_t L, int64_t batch, af_stream stream);
+af_status af_karatsuba_f32(const float* x, const float* y, float* z, int64_t L,
+                           int64_t batch, af_stream stream);
+af_status af_karatsuba_f64(const double* x, const double* y, double* z,
+                           int64_t L, int64_t batch, af_stream stream);
+/* Convolution.Adhoc.cyclic applied to a linear convolution z (batch x 2L-1,
+ * Convolution/Adhoc.hs:104-111): out[k] = z[k] + z[k+L] (batch x L). */
+af_status af_conv_cyclic_fold_i64(const int64_t* z, int64_t* out, int64_t L,
+                                  int64_t batch, af_stream stream);
+af_status af_conv_cyclic_fold_f32(const float* z, float* out, int64_t L,
+                                  int64_t batch, af_stream stream);
+af_status af_conv_cyclic_fold_f64(const double* z, double* out, int64_t L,
+                                  int64_t batch, af_stream stream);
+/* Convolution.Adhoc.complex (Convolution/Adhoc.hs:117-128) over karatsuba
+ * (cyclic = 0: rows of 2L-1) or over `cyclic karatsuba` (cyclic = 1: rows of
+ * L): three real convolutions (re*re, im*im, (re+im)*(re+im)).  Planar. */
+af_status af_conv_complex_i64(int cyclic, const int64_t* x_re, const int64_t* x_im,
+                              const int64_t* y_re, const int64_t* y_im,
+                              int64_t* z_re, int64_t* z_im, int64_t L,
+                              int64_t batch, af_stream stream);
+af_status af_conv_complex_f32(int cyclic, const float* x_re, const float* x_im,
+                              const float* y_re, const float* y_im, float* z_re,
+                              float* z_im, int64_t L, int64_t batch,
+                              af_stream stream);
+af_status af_conv_complex_f64(int cyclic, const double* x_re, const double* x_im,
+                              const double* y_re, const double* y_im,
+                              double* z_re, double* z_im, int64_t L,
+                              int64_t batch, af_stream stream);
 
 /* Power-of-two transform that allocates no device memory.
  * This entry point has no counterpart in the reference.  It serves callers

@@ -1086,6 +1086,9 @@ void or_karatsuba_loop_i64(i64 L, i64 batch, const i64* x, const i64* y, i64* z)
 void or_karatsuba_loop_f64(i64 L, i64 batch, const double* x, const double* y, double* z) {
   karatsuba_loop<double>(L, batch, x, y, z);
 }
+void or_karatsuba_loop_f32(i64 L, i64 batch, const float* x, const float* y, float* z) {
+  karatsuba_loop<float>(L, batch, x, y, z);
+}
 
 // Convolution/Preprocessed.hs:29-56 karatsuba (recursive form), int64
 static void kara_rec(i64 len, const i64* x, const i64* y, i64* z) {

@@ -79,6 +79,7 @@ def lib():
             "or_karatsuba_loop_i64": ([I64, I64, PTR, PTR, PTR], None),
             "or_karatsuba_rec_i64": ([I64, I64, PTR, PTR, PTR], None),
             "or_karatsuba_loop_f64": ([I64, I64, PTR, PTR, PTR], None),
+            "or_karatsuba_loop_f32": ([I64, I64, PTR, PTR, PTR], None),
             "or_cyclic_fold_i64": ([I64, I64, PTR, PTR], None),
             "or_mixed_create": ([ctypes.c_int, ctypes.c_int, I64, PTR], PTR),
             "or_mixed_destroy": ([PTR], None),
@@ -274,6 +275,17 @@ def karatsuba_f64(x, y) -> np.ndarray:
     out = np.zeros(x.shape[:-1] + (max(0, 2 * L - 1),), dtype=np.float64)
     if x.size:
         lib().or_karatsuba_loop_f64(L, batch, _p(x), _p(y), _p(out))
+    return out
+
+
+def karatsuba_f32(x, y) -> np.ndarray:
+    """Convolution.Adhoc.karatsuba over Float rows (loop form, float arithmetic)."""
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    y = np.ascontiguousarray(np.asarray(y, dtype=np.float32))
+    L, batch = _rows(x)
+    out = np.zeros(x.shape[:-1] + (max(0, 2 * L - 1),), dtype=np.float32)
+    if x.size:
+        lib().or_karatsuba_loop_f32(L, batch, _p(x), _p(y), _p(out))
     return out
 
 

@@ -18,6 +18,9 @@ def _lib():
     L.afx_check_plan.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p,
                                  ctypes.c_size_t]
     L.afx_check_plan.restype = ctypes.c_int
+    L.afx_check_axis.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                 ctypes.c_char_p, ctypes.c_size_t]
+    L.afx_check_axis.restype = ctypes.c_int
     L.afx_check_batch.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
     L.afx_check_batch.restype = ctypes.c_int
     return L, _lib.ALGO
@@ -28,6 +31,13 @@ def check_plan(n, sign=-1, algo="auto", batch=1):
     msg = ctypes.create_string_buffer(1024)
     rc = L.afx_check_plan(n, sign, ALGO[algo], batch, msg, len(msg))
     assert rc == 0, (n, algo, batch, msg.value.decode())
+
+
+def check_axis(n, outer, inner, sign=-1, algo="auto"):
+    L, ALGO = _lib()
+    msg = ctypes.create_string_buffer(1024)
+    rc = L.afx_check_axis(n, sign, ALGO[algo], outer, inner, msg, len(msg))
+    assert rc == 0, (n, outer, inner, msg.value.decode())
 
 
 def check_batch(sizes, sign=-1):
@@ -74,3 +84,13 @@ def test_batch_addressing_mixed():
 def test_batch_addressing_benchmark_workload():
     import bench
     check_batch(bench.workload_sizes())
+
+
+# strided-axis programs of the 2-D/3-D transforms: single tiles with
+# line-fast loads, multi-pass schemes through copies (outer > 1) or directly
+@pytest.mark.parametrize("n", [1, 2, 3, 16, 17, 100, 257, 1001, 4096, 4099, 16384, 30011, 65537, 99991])
+def test_axis_addressing(n):
+    for outer, inner in [(1, 1), (1, 7), (3, 5), (2, 64), (1, 256)]:
+        if n * outer * inner <= (1 << 23):
+            check_axis(n, outer, inner)
+    check_axis(n, 2, 3, sign=1)
