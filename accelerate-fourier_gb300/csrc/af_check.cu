@@ -6,7 +6,9 @@
 // formulas and checked against the buffer sizes.  Every element of the
 // output must be written exactly once (the index maps are bijections).  The
 // entry points are internal (afx_*) and used by the CPU test suite.
+#include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -299,6 +301,57 @@ int afx_check_batch(const int64_t* ns, int64_t count, int sign, char* msg, size_
   } catch (const std::exception& e) {
     if (B) batch_destroy(B);
     report(e.what(), msg, len);
+    return -1;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Text summary of a batch program (which: 0 forward, 1 VJP, 2 cotangent),
+// built without a device: one line per launch with its type, threads, CTAs,
+// shared buffer size and the tile descriptors' kinds, lengths and maps.
+int afx_describe_batch(const int64_t* ns, int64_t count, int sign, int which, char* buf, size_t len) {
+  BatchPlan* B = nullptr;
+  try {
+    B = batch_create_mode((const i64*)ns, count, sign, true);
+    const Program& prog = batch_program(B, which);
+    std::string s;
+    for (size_t k = 0; k < prog.launches.size(); ++k) {
+      const Launch& L = prog.launches[k];
+      char line[256];
+      if (L.type == L_MAP) {
+        snprintf(line, sizeof line, "%zu map mode=%d lines=%lld nout=%lld\n", k, L.md.mode, (long long)L.md.nlines,
+                 (long long)L.md.nout);
+        s += line;
+        continue;
+      }
+      i64 elems = 0;
+      std::map<std::string, i64> kinds;
+      for (const WorkItem& it : L.items) {
+        const TileDesc& d = L.descs[it.desc];
+        elems += (i64)it.G * d.slen;
+        char key[96];
+        snprintf(key, sizeof key, "k%d n%d s%d in%d out%d ph%d%s%s", d.kind, d.nlen, d.slen, d.in.map, d.out.map,
+                 d.nph, d.ptw ? " tw" : "", d.in.line_fast || d.out.line_fast ? " lf" : "");
+        kinds[key] += 1;
+      }
+      snprintf(line, sizeof line, "%zu tile T=%d ctas=%zu smem=%d elems=%lld descs=%zu :", k, L.threads,
+               L.items.size(), L.smem_data, (long long)elems, L.descs.size());
+      s += line;
+      int shown = 0;
+      for (auto& kv : kinds) {
+        if (shown++ == 4) { s += " ..."; break; }
+        s += " [" + kv.first + " x" + std::to_string(kv.second) + "]";
+      }
+      s += "\n";
+    }
+    batch_destroy(B);
+    return report(s, buf, len) ? 0 : 0;
+  } catch (const std::exception& e) {
+    if (B) batch_destroy(B);
+    report(e.what(), buf, len);
     return -1;
   }
 }

@@ -26,6 +26,15 @@ static inline FastDiv make_fastdiv(unsigned d) {
   f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
   return f;
 }
+__device__ __forceinline__ FastDiv make_fastdiv_dev(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  if (d <= 1) { f.m = 0; f.s = 0; return f; }
+  const unsigned s = 32 - __clz(d - 1);  // ceil(log2 d)
+  f.s = s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return f;
+}
 __device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
   return f.d <= 1 ? x : ((__umulhi(x, f.m) + x) >> f.s);
 }
@@ -326,19 +335,48 @@ template <> struct Dft<5> {
   }
 };
 
-// Odd prime radix (7, 11, 13): symmetric direct DFT; cos/sin of 2*pi*m/R come
-// from the phase's twiddle table (R divides the phase length n: W_n^(m n/R)).
+// Odd prime radix (7, 11, 13): symmetric direct DFT with the constants
+// cos(2 pi m/R), sin(2 pi m/R), m <= (R-1)/2 (computed in double precision
+// and rounded to float).
+template <int R> struct OddRoots;
+template <> struct OddRoots<7> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[4] = {1.0f, 0.62348980185873359439f, -0.22252093395631433737f, -0.90096886790241903498f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[4] = {0.0f, 0.78183148246802980363f, 0.97492791218182361934f, 0.43388373911755823142f};
+    return v[m];
+  }
+};
+template <> struct OddRoots<11> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[6] = {1.0f, 0.84125353283118120551f, 0.41541501300188643508f, -0.14231483827328500480f,
+                            -0.65486073394528498959f, -0.95949297361449736865f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[6] = {0.0f, 0.54064081745559755543f, 0.90963199535451833011f, 0.98982144188093279524f,
+                            0.75574957435425826890f, 0.28173255684142967104f};
+    return v[m];
+  }
+};
+template <> struct OddRoots<13> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[7] = {1.0f, 0.88545602565320991051f, 0.56806474673115592289f, 0.12053668025532300601f,
+                            -0.35460488704253545489f, -0.74851074817110119231f, -0.97094181742605201180f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[7] = {0.0f, 0.46472317204376850652f, 0.82298386589365635224f, 0.99270887409805397272f,
+                            0.93501624268541483342f, 0.66312265824079519305f, 0.23931566428755768339f};
+    return v[m];
+  }
+};
+
 template <int R> struct DftOdd {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2* tab, int S_log2, int n) {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
     constexpr int h = (R - 1) / 2;
-    float cs[R], sn[R];
-    const int step = n / R;
-#pragma unroll
-    for (int m = 0; m < R; ++m) {
-      float2 w = tw_lookup(tab, S_log2, m * step, -1.0f);  // exp(-2 pi i m/R)
-      cs[m] = w.x;
-      sn[m] = -w.y;  // sin(2 pi m / R)
-    }
     float2 P[h + 1], M[h + 1];
     float2 y0 = u[0];
 #pragma unroll
@@ -354,11 +392,14 @@ template <int R> struct DftOdd {
       float2 a = u[0], b = make_float2(0.f, 0.f);
 #pragma unroll
       for (int j = 1; j <= h; ++j) {
-        int m = (j * k) % R;
-        a.x = fmaf(cs[m], P[j].x, a.x);
-        a.y = fmaf(cs[m], P[j].y, a.y);
-        b.x = fmaf(sn[m], M[j].x, b.x);
-        b.y = fmaf(sn[m], M[j].y, b.y);
+        // cos/sin of 2 pi (j k mod R)/R from the first half (symmetry)
+        const int m = (j * k) % R;
+        const float cm = OddRoots<R>::c(m <= h ? m : R - m);
+        const float sm = m <= h ? OddRoots<R>::s(m) : -OddRoots<R>::s(R - m);
+        a.x = fmaf(cm, P[j].x, a.x);
+        a.y = fmaf(cm, P[j].y, a.y);
+        b.x = fmaf(sm, M[j].x, b.x);
+        b.y = fmaf(sm, M[j].y, b.y);
       }
       float2 ib = mul_si(b, sign);
       out[k] = cadd(a, ib);
@@ -371,3 +412,146 @@ template <int R> struct DftOdd {
 template <> struct Dft<7> : DftOdd<7> {};
 template <> struct Dft<11> : DftOdd<11> {};
 template <> struct Dft<13> : DftOdd<13> {};
+
+// Roots of unity for the composite radices: Roots<R>::c(m) = cos(2 pi m/R),
+// Roots<R>::s(m) = sin(2 pi m/R), m < R (computed in double precision and
+// rounded to float).
+template <int R> struct Roots;
+template <> struct Roots<6> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[6] = {1.00000000000000000000e+00f, 5.00000000000000111022e-01f, -4.99999999999999777955e-01f, -1.00000000000000000000e+00f, -5.00000000000000444089e-01f, 5.00000000000000111022e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[6] = {0.00000000000000000000e+00f, 8.66025403784438596588e-01f, 8.66025403784438707611e-01f, 0.00000000000000000000e+00f, -8.66025403784438374544e-01f, -8.66025403784438596588e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<9> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[9] = {1.00000000000000000000e+00f, 7.66044443118978013452e-01f, 1.73648177666930414453e-01f, -4.99999999999999777955e-01f, -9.39692620785908316883e-01f, -9.39692620785908427905e-01f, -5.00000000000000444089e-01f, 1.73648177666929970364e-01f, 7.66044443118977791407e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[9] = {0.00000000000000000000e+00f, 6.42787609686539251896e-01f, 9.84807753012208020316e-01f, 8.66025403784438707611e-01f, 3.42020143325668879442e-01f, -3.42020143325668657397e-01f, -8.66025403784438374544e-01f, -9.84807753012208131338e-01f, -6.42787609686539584963e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<10> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[10] = {1.00000000000000000000e+00f, 8.09016994374947451263e-01f, 3.09016994374947451263e-01f, -3.09016994374947340241e-01f, -8.09016994374947340241e-01f, -1.00000000000000000000e+00f, -8.09016994374947562285e-01f, -3.09016994374947562285e-01f, 3.09016994374947229218e-01f, 8.09016994374947340241e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[10] = {0.00000000000000000000e+00f, 5.87785252292473137103e-01f, 9.51056516295153531182e-01f, 9.51056516295153642204e-01f, 5.87785252292473248126e-01f, 0.00000000000000000000e+00f, -5.87785252292473026081e-01f, -9.51056516295153531182e-01f, -9.51056516295153642204e-01f, -5.87785252292473359148e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<12> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[12] = {1.00000000000000000000e+00f, 8.66025403784438707611e-01f, 5.00000000000000111022e-01f, 0.00000000000000000000e+00f, -4.99999999999999777955e-01f, -8.66025403784438707611e-01f, -1.00000000000000000000e+00f, -8.66025403784438818633e-01f, -5.00000000000000444089e-01f, 0.00000000000000000000e+00f, 5.00000000000000111022e-01f, 8.66025403784438374544e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[12] = {0.00000000000000000000e+00f, 4.99999999999999944489e-01f, 8.66025403784438596588e-01f, 1.00000000000000000000e+00f, 8.66025403784438707611e-01f, 4.99999999999999944489e-01f, 0.00000000000000000000e+00f, -4.99999999999999722444e-01f, -8.66025403784438374544e-01f, -1.00000000000000000000e+00f, -8.66025403784438596588e-01f, -5.00000000000000444089e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<15> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[15] = {1.00000000000000000000e+00f, 9.13545457642600866599e-01f, 6.69130606358858237570e-01f, 3.09016994374947451263e-01f, -1.04528463267653332069e-01f, -4.99999999999999777955e-01f, -8.09016994374947340241e-01f, -9.78147600733805688833e-01f, -9.78147600733805688833e-01f, -8.09016994374947562285e-01f, -5.00000000000000444089e-01f, -1.04528463267654234126e-01f, 3.09016994374947229218e-01f, 6.69130606358858459615e-01f, 9.13545457642600977621e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[15] = {0.00000000000000000000e+00f, 4.06736643075800152758e-01f, 7.43144825477394133095e-01f, 9.51056516295153531182e-01f, 9.94521895368273400884e-01f, 8.66025403784438707611e-01f, 5.87785252292473248126e-01f, 2.07911690817759314820e-01f, -2.07911690817759065020e-01f, -5.87785252292473026081e-01f, -8.66025403784438374544e-01f, -9.94521895368273289861e-01f, -9.51056516295153642204e-01f, -7.43144825477394022073e-01f, -4.06736643075800152758e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<20> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[20] = {1.00000000000000000000e+00f, 9.51056516295153531182e-01f, 8.09016994374947451263e-01f, 5.87785252292473137103e-01f, 3.09016994374947451263e-01f, 0.00000000000000000000e+00f, -3.09016994374947340241e-01f, -5.87785252292473026081e-01f, -8.09016994374947340241e-01f, -9.51056516295153531182e-01f, -1.00000000000000000000e+00f, -9.51056516295153753227e-01f, -8.09016994374947562285e-01f, -5.87785252292473248126e-01f, -3.09016994374947562285e-01f, 0.00000000000000000000e+00f, 3.09016994374947229218e-01f, 5.87785252292472915059e-01f, 8.09016994374947340241e-01f, 9.51056516295153531182e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[20] = {0.00000000000000000000e+00f, 3.09016994374947395752e-01f, 5.87785252292473137103e-01f, 8.09016994374947451263e-01f, 9.51056516295153531182e-01f, 1.00000000000000000000e+00f, 9.51056516295153642204e-01f, 8.09016994374947451263e-01f, 5.87785252292473248126e-01f, 3.09016994374947506774e-01f, 0.00000000000000000000e+00f, -3.09016994374946896151e-01f, -5.87785252292473026081e-01f, -8.09016994374947340241e-01f, -9.51056516295153531182e-01f, -1.00000000000000000000e+00f, -9.51056516295153642204e-01f, -8.09016994374947562285e-01f, -5.87785252292473359148e-01f, -3.09016994374947617796e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<25> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[25] = {1.00000000000000000000e+00f, 9.68583161128631076053e-01f, 8.76306680043863583940e-01f, 7.28968627421411552447e-01f, 5.35826794978996545638e-01f, 3.09016994374947451263e-01f, 6.27905195293135265366e-02f, -1.87381314585724600974e-01f, -4.25779291565072715020e-01f, -6.37423989748689745483e-01f, -8.09016994374947340241e-01f, -9.29776485888251347234e-01f, -9.92114701314477764882e-01f, -9.92114701314477875904e-01f, -9.29776485888251458256e-01f, -8.09016994374947784330e-01f, -6.37423989748689523438e-01f, -4.25779291565072159909e-01f, -1.87381314585724628730e-01f, 6.27905195293128326472e-02f, 3.09016994374947229218e-01f, 5.35826794978996767682e-01f, 7.28968627421411219380e-01f, 8.76306680043863139851e-01f, 9.68583161128630965031e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[25] = {0.00000000000000000000e+00f, 2.48689887164854794843e-01f, 4.81753674101715323452e-01f, 6.84547105928688615073e-01f, 8.44327925502015075310e-01f, 9.51056516295153531182e-01f, 9.98026728428271558968e-01f, 9.82287250728688721146e-01f, 9.04827052466019465804e-01f, 7.70513242775789253258e-01f, 5.87785252292473248126e-01f, 3.68124552684678141290e-01f, 1.25333233564304535879e-01f, -1.25333233564304286078e-01f, -3.68124552684677919245e-01f, -5.87785252292472693014e-01f, -7.70513242775789364281e-01f, -9.04827052466019798871e-01f, -9.82287250728688721146e-01f, -9.98026728428271558968e-01f, -9.51056516295153642204e-01f, -8.44327925502014964287e-01f, -6.84547105928688948140e-01f, -4.81753674101716100608e-01f, -2.48689887164855349955e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<27> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[27] = {1.00000000000000000000e+00f, 9.73044870579823806267e-01f, 8.93632640323412275052e-01f, 7.66044443118978013452e-01f, 5.97158591702786178956e-01f, 3.96079766039156899726e-01f, 1.73648177666930414453e-01f, -5.81448289104757737311e-02f, -2.86803232711090205775e-01f, -4.99999999999999777955e-01f, -6.86241637868733489469e-01f, -8.35487811412936265398e-01f, -9.39692620785908316883e-01f, -9.93238357741943023171e-01f, -9.93238357741943023171e-01f, -9.39692620785908538927e-01f, -8.35487811412936487443e-01f, -6.86241637868733600492e-01f, -5.00000000000000444089e-01f, -2.86803232711090649865e-01f, -5.81448289104762386370e-02f, 1.73648177666930830787e-01f, 3.96079766039156511148e-01f, 5.97158591702785845889e-01f, 7.66044443118977791407e-01f, 8.93632640323412164030e-01f, 9.73044870579824028312e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[27] = {0.00000000000000000000e+00f, 2.30615870742440165486e-01f, 4.48799180200462166646e-01f, 6.42787609686539251896e-01f, 8.02123192755043734614e-01f, 9.18216106880273996715e-01f, 9.84807753012208020316e-01f, 9.98308158271268175632e-01f, 9.57989512315488900285e-01f, 8.66025403784438707611e-01f, 7.27373641573048845821e-01f, 5.49508978070806231031e-01f, 3.42020143325668879442e-01f, 1.16092914125229929034e-01f, -1.16092914125230123323e-01f, -3.42020143325668213308e-01f, -5.49508978070806008986e-01f, -7.27373641573048623776e-01f, -8.66025403784438374544e-01f, -9.57989512315488789262e-01f, -9.98308158271268175632e-01f, -9.84807753012208020316e-01f, -9.18216106880274107738e-01f, -8.02123192755043956659e-01f, -6.42787609686539584963e-01f, -4.48799180200462444201e-01f, -2.30615870742439582619e-01f};
+    return v[m];
+  }
+};
+template <> struct Roots<32> {
+  static __device__ __forceinline__ float c(int m) {
+    constexpr float v[32] = {1.00000000000000000000e+00f, 9.80785280403230430579e-01f, 9.23879532511286738483e-01f, 8.31469612302545235671e-01f, 7.07106781186547572737e-01f, 5.55570233019602288671e-01f, 3.82683432365089837290e-01f, 1.95090322016128331351e-01f, 0.00000000000000000000e+00f, -1.95090322016128192573e-01f, -3.82683432365089726268e-01f, -5.55570233019601955604e-01f, -7.07106781186547461715e-01f, -8.31469612302545346694e-01f, -9.23879532511286738483e-01f, -9.80785280403230430579e-01f, -1.00000000000000000000e+00f, -9.80785280403230430579e-01f, -9.23879532511286849505e-01f, -8.31469612302545457716e-01f, -7.07106781186547683760e-01f, -5.55570233019602177649e-01f, -3.82683432365090336891e-01f, -1.95090322016128664417e-01f, 0.00000000000000000000e+00f, 1.95090322016128303595e-01f, 3.82683432365090003824e-01f, 5.55570233019601844582e-01f, 7.07106781186547350693e-01f, 8.31469612302545235671e-01f, 9.23879532511286516439e-01f, 9.80785280403230319557e-01f};
+    return v[m];
+  }
+  static __device__ __forceinline__ float s(int m) {
+    constexpr float v[32] = {0.00000000000000000000e+00f, 1.95090322016128248084e-01f, 3.82683432365089781779e-01f, 5.55570233019602177649e-01f, 7.07106781186547461715e-01f, 8.31469612302545235671e-01f, 9.23879532511286738483e-01f, 9.80785280403230430579e-01f, 1.00000000000000000000e+00f, 9.80785280403230430579e-01f, 9.23879532511286738483e-01f, 8.31469612302545457716e-01f, 7.07106781186547572737e-01f, 5.55570233019602177649e-01f, 3.82683432365089892802e-01f, 1.95090322016128608906e-01f, 0.00000000000000000000e+00f, -1.95090322016128359106e-01f, -3.82683432365089670757e-01f, -5.55570233019601955604e-01f, -7.07106781186547461715e-01f, -8.31469612302545235671e-01f, -9.23879532511286516439e-01f, -9.80785280403230319557e-01f, -1.00000000000000000000e+00f, -9.80785280403230430579e-01f, -9.23879532511286627461e-01f, -8.31469612302545457716e-01f, -7.07106781186547683760e-01f, -5.55570233019602177649e-01f, -3.82683432365090392402e-01f, -1.95090322016128719929e-01f};
+    return v[m];
+  }
+};
+
+// multiply by exp(sign * 2 pi i m / R) for a compile-time m (after unrolling)
+template <int R>
+__device__ __forceinline__ float2 mul_root(float2 a, int m, float sign) {
+  m %= R;
+  if (m == 0) return a;
+  if (4 * m == R) return mul_si(a, sign);
+  if (2 * m == R) return make_float2(-a.x, -a.y);
+  if (4 * m == 3 * R) return mul_si(a, -sign);
+  return cmul(a, make_float2(Roots<R>::c(m), sign * Roots<R>::s(m)));
+}
+
+// Composite radix R = A*B (Cooley-Tukey inside the butterfly): DFT_A over j1
+// of u[B j1 + j2], twiddle W_R^(j2 k1), DFT_B over j2; output k1 + A k2.
+template <int A, int B>
+struct DftComposite {
+  static __device__ __forceinline__ void run(float2* u, float sign, const float2* tab, int S, int n) {
+    constexpr int R = A * B;
+    float2 v[R];
+#pragma unroll
+    for (int j2 = 0; j2 < B; ++j2) {
+      float2 t[A];
+#pragma unroll
+      for (int j1 = 0; j1 < A; ++j1) t[j1] = u[B * j1 + j2];
+      Dft<A>::run(t, sign, tab, S, n);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) v[j2 * A + k1] = mul_root<R>(t[k1], j2 * k1, sign);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      float2 t[B];
+#pragma unroll
+      for (int j2 = 0; j2 < B; ++j2) t[j2] = v[j2 * A + k1];
+      Dft<B>::run(t, sign, tab, S, n);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) u[k1 + A * k2] = t[k2];
+    }
+  }
+};
+template <> struct Dft<6> : DftComposite<2, 3> {};
+template <> struct Dft<9> : DftComposite<3, 3> {};
+template <> struct Dft<10> : DftComposite<2, 5> {};
+template <> struct Dft<12> : DftComposite<4, 3> {};
+template <> struct Dft<15> : DftComposite<3, 5> {};
+template <> struct Dft<20> : DftComposite<4, 5> {};
+template <> struct Dft<25> : DftComposite<5, 5> {};
+template <> struct Dft<27> : DftComposite<3, 9> {};
+template <> struct Dft<32> : DftComposite<4, 8> {};

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <functional>
 
 namespace af {
 
@@ -261,16 +262,44 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
 // elements per CTA the ping-pong tile can hold (two padded buffers + tables)
 static const i64 kTileCap = 13000;
 
+// Radix sequence of a tile phase: the fewest Stockham passes over the
+// supported butterflies (prime radices 2..13 and the composites built from
+// them), ties going to the smaller largest radix; largest radix first, so
+// the pass without twiddles carries the most elements per butterfly.
+static const int kRadices[] = {2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 15, 16, 20, 25, 27};
 static std::vector<int> radices(i64 n) {
+  static std::map<i64, std::vector<int>> memo;
+  auto it = memo.find(n);
+  if (it != memo.end()) return it->second;
+  // best[d] over the divisors d of n: (passes, sum of radices) and the radix used
+  std::vector<i64> divs;
+  for (i64 d = 1; d * d <= n; ++d)
+    if (n % d == 0) { divs.push_back(d); if (d != n / d) divs.push_back(n / d); }
+  std::sort(divs.begin(), divs.end());
+  std::map<i64, std::pair<std::pair<int, int>, int>> best;
+  best[1] = {{0, 0}, 0};
+  for (i64 d : divs) {
+    if (d == 1) continue;
+    std::pair<std::pair<int, int>, int> b{{1 << 30, 0}, 0};
+    for (int R : kRadices) {
+      if (d % R) continue;
+      auto sub = best.find(d / R);
+      if (sub == best.end() || sub->second.first.first >= (1 << 30)) continue;
+      std::pair<int, int> c{sub->second.first.first + 1, sub->second.first.second + R};
+      if (c < b.first) b = {c, R};
+    }
+    best[d] = b;
+  }
   std::vector<int> r;
-  int a = 0;
-  while (n % 2 == 0) { n /= 2; ++a; }
-  while (a >= 4) { r.push_back(16); a -= 4; }
-  if (a == 3) r.push_back(8);
-  else if (a == 2) r.push_back(4);
-  else if (a == 1) r.push_back(2);
-  for (int p : {3, 5, 7, 11, 13})
-    while (n % p == 0) { r.push_back(p); n /= p; }
+  i64 m = n;
+  while (m > 1) {
+    const auto& b = best[m];
+    if (b.first.first >= (1 << 30)) throw AfError(AF_ERR_UNSUPPORTED, "length is not 13-smooth");
+    r.push_back(b.second);
+    m /= b.second;
+  }
+  std::sort(r.begin(), r.end(), std::greater<int>());
+  memo[n] = r;
   return r;
 }
 

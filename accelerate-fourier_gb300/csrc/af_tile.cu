@@ -4,9 +4,9 @@
 // per CTA, each naming a tile descriptor (device memory) and the lines it
 // owns.  A CTA copies its descriptor to shared memory, loads its lines
 // through the descriptor's index map, runs one or two Stockham FFT phases
-// (passes of radix 2,3,4,5,7,8,11,13,16 alternating between two shared
-// buffers), and stores through the inverse map with the four-step twiddle,
-// scale and optional cotangent epilogue.
+// (passes of radix 2 to 27 alternating between two shared buffers), and
+// stores through the inverse map with the four-step twiddle, scale and
+// optional cotangent epilogue.
 //
 // Tile kinds restate the reference's algorithms (file:line relative to the
 // accelerate-fourier project):
@@ -22,49 +22,76 @@
 
 namespace af {
 
-// Scalars of one pass, held in registers: the descriptors live in shared
-// memory, which the passes write, so every field read in a loop would
-// otherwise be re-read from shared memory each iteration.
-struct PassRegs {
-  int n, nb, lines, LS, ls, es, lcnt, p, tw_stride, S_log2;
+// Scalars of one phase, held in registers (the descriptor lives in shared
+// memory; reading its fields inside the pass loops would re-read them).
+struct PhaseRegs {
+  int n, lines, LS, ls, es, lcnt, S_log2;
   float sign;
-  FastDiv nb_div, p_div, lcnt_div;
+  FastDiv lcnt_div;
 };
 
-// One Stockham pass, src -> dst (ping-pong shared buffers): each thread
-// walks butterflies g = tid, tid + T, ... holding one radix-R butterfly.
+
+// u[j] *= w1^j for j = 1..R-1.  The powers are built as w^(Q a + b) =
+// (w^Q)^a * w^b from the small powers w^b (b < Q) and w^Q, so that at most a
+// handful of complex values are live and no power is more than five
+// products deep.
+template <int R>
+__device__ __forceinline__ void apply_twiddles(float2* u, float2 w1) {
+  constexpr int Q = R <= 4 ? 2 : (R <= 9 ? 3 : 4);
+  float2 s[Q];
+  s[0] = make_float2(1.f, 0.f);
+  s[1] = w1;
+#pragma unroll
+  for (int b = 2; b < Q; ++b) s[b] = b == 2 ? cmul(w1, w1) : cmul(s[b - 1], w1);
+  const float2 big = Q == 2 ? cmul(w1, w1) : (Q == 4 ? cmul(s[2], s[2]) : cmul(s[2], w1));  // w^Q
+  float2 base = big;
+#pragma unroll
+  for (int j = 1; j < R; ++j) {
+    const int a = j / Q, b = j % Q;
+    if (a >= 2 && b == 0) base = a == 2 ? cmul(big, big) : cmul(base, big);
+    const float2 w = a == 0 ? s[b] : (b == 0 ? base : cmul(base, s[b]));
+    u[j] = cmul(u[j], w);
+  }
+}
+
+// One Stockham pass, src -> dst (ping-pong shared buffers).  Butterfly g (of
+// the phase's lines*n/R) reads elements i + j*(n/R) of its line, applies the
+// twiddles W^(j k tw_stride) (k = i mod p) and the radix-R DFT, and writes
+// (i-k)*R + k + j*p.
 template <int R, int T>
 __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, float2* __restrict__ dst,
-                                              const PassRegs r, const float2* __restrict__ ptab) {
-  const int total = r.lines * r.nb;
+                                              const PhaseRegs& ph, const PassDesc& pd,
+                                              const float2* __restrict__ ptab) {
+  const int nb = ph.n / R;
+  const int total = ph.lines * nb;
+  const int p = pd.p, tws = pd.tw_stride;
+  const FastDiv nbd = pd.nb_div, pdv = pd.p_div;
+  const int pe = p * ph.es, nbe = nb * ph.es;
   for (int g = threadIdx.x; g < total; g += T) {
-    const int l = (int)fdiv((unsigned)g, r.nb_div);
-    const int i = g - l * r.nb;
-    const int t = (int)fdiv((unsigned)l, r.lcnt_div);
-    const int base = t * r.LS + (l - t * r.lcnt) * r.ls;
+    const int l = (int)fdiv((unsigned)g, nbd);
+    const int i = g - l * nb;
+    const int t = (int)fdiv((unsigned)l, ph.lcnt_div);
+    const int base = t * ph.LS + (l - t * ph.lcnt) * ph.ls;
     float2 u[R];
+    const int ib = base + i * ph.es;
 #pragma unroll
-    for (int j = 0; j < R; ++j) u[j] = src[spad(base + (i + j * r.nb) * r.es)];
-    const int q = (int)fdiv((unsigned)i, r.p_div);
-    const int k = i - q * r.p;
-    if (k > 0) {
-      const int st = k * r.tw_stride;
+    for (int j = 0; j < R; ++j) u[j] = src[spad(ib + j * nbe)];
+    const int q = (int)fdiv((unsigned)i, pdv);
+    const int k = i - q * p;
+    if (k > 0) apply_twiddles<R>(u, tw_lookup(ptab, ph.S_log2, k * tws, ph.sign));
+    Dft<R>::run(u, ph.sign, ptab, ph.S_log2, ph.n);
+    const int ob = base + (q * p * R + k) * ph.es;
 #pragma unroll
-      for (int j = 1; j < R; ++j) u[j] = cmul(u[j], tw_lookup(ptab, r.S_log2, j * st, r.sign));
-    }
-    Dft<R>::run(u, r.sign, ptab, r.S_log2, r.n);
-    const int ob = q * r.p * R + k;
-#pragma unroll
-    for (int j = 0; j < R; ++j) dst[spad(base + (ob + j * r.p) * r.es)] = u[j];
+    for (int j = 0; j < R; ++j) dst[spad(ob + j * pe)] = u[j];
   }
   __syncthreads();
 }
 
 // Runs every pass of a phase; returns the buffer holding the result.
 template <int T>
-__device__ __noinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
-                                          const float2* tab) {
-  PassRegs r;
+__device__ __forceinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
+                                             const float2* tab) {
+  PhaseRegs r;
   r.n = phs->n;
   r.lines = G * phs->lcnt;
   r.LS = LS;
@@ -78,21 +105,24 @@ __device__ __noinline__ float2* run_phase(float2* cur, float2* oth, const FftPha
   const int npass = phs->npass;
   for (int p = 0; p < npass; ++p) {
     const PassDesc pd = phs->pass[p];
-    r.nb = r.n / pd.R;
-    r.p = pd.p;
-    r.tw_stride = pd.tw_stride;
-    r.nb_div = pd.nb_div;
-    r.p_div = pd.p_div;
     switch (pd.R) {
-      case 2: stockham_pass<2, T>(cur, oth, r, ptab); break;
-      case 3: stockham_pass<3, T>(cur, oth, r, ptab); break;
-      case 4: stockham_pass<4, T>(cur, oth, r, ptab); break;
-      case 5: stockham_pass<5, T>(cur, oth, r, ptab); break;
-      case 7: stockham_pass<7, T>(cur, oth, r, ptab); break;
-      case 8: stockham_pass<8, T>(cur, oth, r, ptab); break;
-      case 11: stockham_pass<11, T>(cur, oth, r, ptab); break;
-      case 13: stockham_pass<13, T>(cur, oth, r, ptab); break;
-      case 16: stockham_pass<16, T>(cur, oth, r, ptab); break;
+      case 2: stockham_pass<2, T>(cur, oth, r, pd, ptab); break;
+      case 3: stockham_pass<3, T>(cur, oth, r, pd, ptab); break;
+      case 4: stockham_pass<4, T>(cur, oth, r, pd, ptab); break;
+      case 5: stockham_pass<5, T>(cur, oth, r, pd, ptab); break;
+      case 6: stockham_pass<6, T>(cur, oth, r, pd, ptab); break;
+      case 7: stockham_pass<7, T>(cur, oth, r, pd, ptab); break;
+      case 8: stockham_pass<8, T>(cur, oth, r, pd, ptab); break;
+      case 9: stockham_pass<9, T>(cur, oth, r, pd, ptab); break;
+      case 10: stockham_pass<10, T>(cur, oth, r, pd, ptab); break;
+      case 11: stockham_pass<11, T>(cur, oth, r, pd, ptab); break;
+      case 12: stockham_pass<12, T>(cur, oth, r, pd, ptab); break;
+      case 13: stockham_pass<13, T>(cur, oth, r, pd, ptab); break;
+      case 15: stockham_pass<15, T>(cur, oth, r, pd, ptab); break;
+      case 16: stockham_pass<16, T>(cur, oth, r, pd, ptab); break;
+      case 20: stockham_pass<20, T>(cur, oth, r, pd, ptab); break;
+      case 25: stockham_pass<25, T>(cur, oth, r, pd, ptab); break;
+      case 27: stockham_pass<27, T>(cur, oth, r, pd, ptab); break;
     }
     float2* tmp = cur;
     cur = oth;
@@ -251,7 +281,7 @@ __device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, float2
 
 template <int T>
 __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it, const TileBases& B,
-                                          float2* A, float2* Bf, float2* tab, float2* xs, double* loss) {
+                                          float2* A, float2* Bf, const float2* tab, float2* xs, double* loss) {
   const int line0 = it.line0;
   const int G = it.G;
   const int N = d.nlen;
@@ -269,21 +299,45 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   const i64 ibase = in.off + it.in_add;
   const i64 obase = out.off + it.out_add;
 
+  // Per-line base offsets of AFFINE views (hi*s_hi + lo*s_lo, relative to
+  // the view's offset) for the CTA's G lines, input then output; PLAIN and
+  // CONVROW tiles keep them in the per-line scratch (16 bytes per line).
+  const bool rows_kind = d.kind == TILE_PLAIN || d.kind == TILE_CONVROW;
+  i64* lbi = reinterpret_cast<i64*>(xs);
+  i64* lbo = lbi + G;
+  if (rows_kind) {
+    for (int l = threadIdx.x; l < G; l += T) {
+      int hi, lo;
+      split_line(in, line0 + l, hi, lo);
+      lbi[l] = (i64)hi * in.s_hi + (i64)lo * in.s_lo;
+      split_line(out, line0 + l, hi, lo);
+      lbo[l] = (i64)hi * out.s_hi + (i64)lo * out.s_lo;
+    }
+    __syncthreads();
+  }
+  float lsum = 0.f;
+
   // ------------------------------------------------------------ load
   // Loads are issued in groups of U independent read-only-path loads per
   // thread before any shared-memory write, so that many are in flight.
   const int LS = d.LS;
-  if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
+  if (rows_kind) {
     const IoRegs r = io_regs(in, B, ibase);
     const int lf = in.line_fast;
     switch (in.map) {
       case IO_AFFINE:
-        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
-          int hi, lo;
-          rsplit(r, line0 + l, hi, lo);
-          v = rld(r, (i64)hi * r.s_hi + (i64)lo * r.s_lo + (i64)e * r.s_e);
-          return spad(l * LS + e);
-        }, sm);
+        if (r.s_e == 1) {
+          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+            v = rld(r, lbi[l] + e);
+            return spad(l * LS + e);
+          }, sm);
+        } else {
+          const i64 se = r.s_e;
+          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+            v = rld(r, lbi[l] + (i64)e * se);
+            return spad(l * LS + e);
+          }, sm);
+        }
         break;
       case IO_GT:
         load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
@@ -399,7 +453,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
 
   // ------------------------------------------------------------ store
   StoreCtx sc{&B, 0.f, d.cot};
-  if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
+  if (rows_kind) {
     const IoRegs ro = io_regs(out, B, obase);
     const float2* __restrict__ ptw = d.ptw;
     const int ptwS = d.ptwS_log2;
@@ -413,7 +467,6 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     const float2* x0p = B.c[out.x0_buf] + out.x0_off + (out.x0_buf == in.buf ? it.in_add : it.out_add);
     const i64 x0_shi = out.x0_shi;
     const float2* dcp = B.c[BUF_WS] + out.dc_off + it.in_add;
-    float lsum = 0.f;
     auto put = [&](i64 rel, float2 v) {
       if (cot) {
         const float w = __ldg(&wp[obase + rel]);
@@ -423,9 +476,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       if (ro.c) ro.c[rel] = v;
       else { ro.re[rel] = v.x; ro.im[rel] = v.y; }
     };
+    const i64 ose = ro.s_e;
     for_tile<T>(G, N, d.N_div, Gdiv, out.line_fast, [&](int l, int e) {
       int hi, lo;
-      rsplit(ro, line0 + l, hi, lo);
+      if (omap == IO_AFFINE && !ptw) {
+        hi = lo = 0;
+      } else {
+        rsplit(ro, line0 + l, hi, lo);
+      }
       float2 v = sm[spad(l * LS + e)];
       if (ptw) {
         const unsigned t = mulmod((unsigned)lo, (unsigned)e, pmod);
@@ -436,10 +494,12 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         v = cmul(v, w);
       }
       v = cscale(v, scale);
-      const i64 hb = (i64)hi * ro.s_hi;
       if (omap == IO_AFFINE) {
-        put(hb + (i64)lo * ro.s_lo + (i64)e * ro.s_e, v);
-      } else if (omap == IO_GT) {
+        put(lbo[l] + (i64)e * ose, v);
+        return;
+      }
+      const i64 hb = (i64)hi * ro.s_hi;
+      if (omap == IO_GT) {
         put(hb + (i64)rgt(ro, lo, e) * ro.s_t, v);
       } else if (omap == IO_CHIRP) {
         const i64 q = lo * ro.q_lo + e * ro.q_e;
