@@ -106,7 +106,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (OSError, FileNotFoundError):
@@ -210,16 +210,34 @@ class BatchRunner:
     def __init__(self, ns):
         from accelerate_fourier import _lib
         self.batch = _lib.Batch(ns, -1)
-        self.launches_per_step = 2 * self.batch.launches() + 1  # + the loss reset
+        self.launches_per_step = 2 * self.batch.launches()  # tile kernels (the loss reset is a memset)
 
     def step(self, x, w, cot, grad, loss, stream):
         self.batch.forward_cotangent_ptr(x.data_ptr(), w.data_ptr(), cot.data_ptr(), loss.data_ptr(), stream)
         self.batch.vjp_ptr(cot.data_ptr(), grad.data_ptr(), stream)
 
 
-def time_steps(fn, steps, warmup, torch):
+def max_over_ranks(v: float, dist=None) -> float:
+    """The largest value over all ranks (the job's time is its slowest
+    rank's); v itself when not distributed."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return v
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def time_steps(fn, steps, warmup, torch, dist=None):
+    """CUDA-event time per step on the launching stream, after `warmup`
+    untimed steps, with a barrier and a device synchronize on both sides of
+    the timed region; the maximum over ranks."""
     for _ in range(warmup):
         fn()
+    torch.cuda.synchronize()
+    if dist is not None and dist.is_initialized():
+        dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -227,12 +245,29 @@ def time_steps(fn, steps, warmup, torch):
         fn()
     e1.record()
     torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / steps
+    if dist is not None and dist.is_initialized():
+        dist.barrier()
+    return max_over_ranks(e0.elapsed_time(e1) / steps, dist)
+
+
+def dist_setup(torch):
+    """One process per GPU under torchrun (RANK / LOCAL_RANK / WORLD_SIZE);
+    the collectives only synchronize the timing: the transforms are replicas
+    with no exchange."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local if world > 1 else 0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        return rank, world, dist
+    return 0, 1, None
 
 
 def run_ours(args):
     import torch
-    torch.cuda.set_device(0)
+    rank, world, dist = dist_setup(torch)
     ns = workload_sizes(args.count)
     total = int(ns.sum())
     nbytes = 32 * total
@@ -259,17 +294,18 @@ def run_ours(args):
         step()
     torch.cuda.synchronize()
 
-    clocks = ClockSampler()
+    clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    ms = time_steps(graph.replay, args.steps, args.warmup, torch)
+    ms = time_steps(graph.replay, args.steps, args.warmup, torch, dist)
     clk = clocks.stop()
 
     # per-launch timing of the two halves (forward+cotangent, VJP)
     ms_fwd = time_steps(lambda: runner.batch.forward_cotangent_ptr(
         x.data_ptr(), w.data_ptr(), cot.data_ptr(), loss.data_ptr(), torch.cuda.current_stream().cuda_stream),
-        args.steps, 2, torch)
+        args.steps, 2, torch, dist)
     ms_vjp = time_steps(lambda: runner.batch.vjp_ptr(cot.data_ptr(), grad.data_ptr(),
-                                                     torch.cuda.current_stream().cuda_stream), args.steps, 2, torch)
+                                                     torch.cuda.current_stream().cuda_stream), args.steps, 2, torch,
+                        dist)
 
     # end to end: pinned host inputs, H2D + step + D2H of the gradient and loss
     xpin = torch.from_numpy(xh).pin_memory()
@@ -284,11 +320,11 @@ def run_ours(args):
         gpin.copy_(grad, non_blocking=True)
         lpin.copy_(loss, non_blocking=True)
 
-    ms_e2e = time_steps(e2e_step, args.steps, 2, torch)
+    ms_e2e = time_steps(e2e_step, args.steps, 2, torch, dist)
 
     # plain path (one plan exec per transform) for the "vs plain" ratio
     ms_plain = None
-    if not args.skip_plain:
+    if not args.skip_plain and world == 1:
         plain = PlainRunner(ns)
         xs_ = torch.cuda.current_stream().cuda_stream
 
@@ -299,6 +335,10 @@ def run_ours(args):
 
         ms_plain = time_steps(plain_step, 2, 1, torch)
 
+    if rank != 0:
+        dist.barrier()
+        dist.destroy_process_group()
+        return
     # accuracy vs the FP64 oracle on a sample of transforms
     from oracle import oracle as O
     step()
@@ -312,7 +352,8 @@ def run_ours(args):
         ref = 2 * wh[o:o + n] * X
         errs.append(np.linalg.norm(ch[o:o + n] - ref) / np.linalg.norm(ref))
 
-    value = nbytes / (ms * 1e-3) / 1e9
+    # whole-job throughput: every rank transforms its own copy of the workload
+    value = world * nbytes / (ms * 1e-3) / 1e9
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -321,34 +362,38 @@ def run_ours(args):
     alg_bytes = total * (8 + 4 + 8 + 8 + 8)
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         v, cores, sample = cpu_baseline(ns)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
         "config": {"workload": "4096 mixed-size C2C transforms, n log-uniform [16, 65536] "
                                "(50% 5-smooth, 25% prime, 25% raw), fwd + cotangent + VJP",
                    "sum_n": total, "path": "batched executor, CUDA graph",
+                   "parallelism": f"replicas x{world} (no exchange)",
                    "l2": "inputs (267 MB) larger than L2",
                    "bytes_credited_per_step": "32 * sum(n) (16 N per transform application)",
                    "ms_forward_cotangent": ms_fwd, "ms_vjp": ms_vjp,
                    "plain_ms_per_step": ms_plain, "speedup_vs_plain": (ms_plain / ms) if ms_plain else None},
-        "e2e": {"value": nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+        "e2e": {"value": world * nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(xh.nbytes + wh.nbytes), "d2h_bytes_per_step": int(xh.nbytes + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": "tile kernel over the whole step: algorithmic 36 B per point "
                              "(x, w, g, g, grad) / step time; peak = measured copy bandwidth"},
         "cpu_baseline": cpu,
-        "gpu_launches": runner.launches_per_step * args.steps,
+        "gpu_launches": runner.launches_per_step * args.steps * world,
         "clocks": clk,
         "err_vs_fp64": {"max_rel_l2": float(max(errs)), "median_rel_l2": float(np.median(errs)),
                         "sample": f"{len(errs)} transforms"},
         "loss": float(loss.item()),
     }
     print(json.dumps(out))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 def run_reference(args):
