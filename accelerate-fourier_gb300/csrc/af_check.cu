@@ -320,7 +320,7 @@ int afx_describe_batch(const int64_t* ns, int64_t count, int sign, int which, ch
     std::string s;
     for (size_t k = 0; k < prog.launches.size(); ++k) {
       const Launch& L = prog.launches[k];
-      char line[256];
+      char line[512];
       if (L.type == L_MAP) {
         snprintf(line, sizeof line, "%zu map mode=%d lines=%lld nout=%lld\n", k, L.md.mode, (long long)L.md.nlines,
                  (long long)L.md.nout);
@@ -342,7 +342,7 @@ int afx_describe_batch(const int64_t* ns, int64_t count, int sign, int which, ch
       s += line;
       int shown = 0;
       for (auto& kv : kinds) {
-        if (shown++ == 4) { s += " ..."; break; }
+        if (shown++ == 400) { s += " ..."; break; }
         s += " [" + kv.first + " x" + std::to_string(kv.second) + "]";
       }
       s += "\n";

@@ -69,6 +69,10 @@ static void fft64(const cd* x, i64 xs, cd* y, i64 n, int sign) {
 void PlanRes::release() {
   for (void* p : allocs) cudaFree(p);
   allocs.clear();
+  for (cudaStream_t t : streams) cudaStreamDestroy(t);
+  streams.clear();
+  for (cudaEvent_t e : events) cudaEventDestroy(e);
+  events.clear();
   tables.clear();
   pair_tables.clear();
   rader.clear();
@@ -871,7 +875,32 @@ static void append_tile(Launch& L, const TileStep& s, int desc_index, i64 in_add
 
 int Program::tile_launches() const { return (int)launches.size(); }
 
+// Side streams and events of a concurrent program (fork-join on the
+// caller's stream; under stream capture the branches become parallel graph
+// nodes).
+static void make_program_streams(PlanRes& res, Program& prog) {
+  if (prog.nstreams <= 1 || res.dry || res.no_alloc) {
+    prog.nstreams = 1;
+    return;
+  }
+  for (int i = 1; i < prog.nstreams; ++i) {
+    cudaStream_t t;
+    cuda_check(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking), "side stream");
+    res.streams.push_back(t);
+    prog.side.push_back(t);
+  }
+  // one event per launch, then the fork event and one join event per side stream
+  const size_t nev = prog.launches.size() + (size_t)prog.nstreams;
+  for (size_t i = 0; i < nev; ++i) {
+    cudaEvent_t e;
+    cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "program event");
+    res.events.push_back(e);
+    prog.ev.push_back(e);
+  }
+}
+
 void finalize_program(PlanRes& res, Program& prog) {
+  make_program_streams(res, prog);
   size_t bytes = 0;
   for (Launch& L : prog.launches) {
     if (L.type != L_TILE) continue;
@@ -920,22 +949,49 @@ TileBases make_bases(const float* in_re, const float* in_im, float* out_re, floa
   return b;
 }
 
+static cudaError_t run_launch(const Program& prog, const Launch& L, const TileBases& bases, double* loss,
+                              cudaStream_t st) {
+  if (L.type == L_TILE) {
+    LaunchSpec spec;
+    spec.descs = reinterpret_cast<const TileDesc*>(prog.dblob + L.desc_off);
+    spec.items = reinterpret_cast<const WorkItem*>(prog.dblob + L.item_off);
+    spec.nitems = (int)L.items.size();
+    spec.threads = L.threads;
+    spec.smem_data = L.smem_data;
+    spec.smem_bytes = tile_smem_bytes(L.smem_data, kMaxTw, kMaxG);
+    return launch_tiles(spec, bases, loss, st);
+  }
+  return launch_map(L.md, bases, st);
+}
+
 cudaError_t run_program(const Program& prog, const TileBases& bases, double* loss, cudaStream_t st) {
-  for (const Launch& L : prog.launches) {
-    cudaError_t e;
-    if (L.type == L_TILE) {
-      LaunchSpec spec;
-      spec.descs = reinterpret_cast<const TileDesc*>(prog.dblob + L.desc_off);
-      spec.items = reinterpret_cast<const WorkItem*>(prog.dblob + L.item_off);
-      spec.nitems = (int)L.items.size();
-      spec.threads = L.threads;
-      spec.smem_data = L.smem_data;
-      spec.smem_bytes = tile_smem_bytes(L.smem_data, kMaxTw, kMaxG);
-      e = launch_tiles(spec, bases, loss, st);
-    } else {
-      e = launch_map(L.md, bases, st);
-    }
-    if (e != cudaSuccess) return e;
+  const size_t nl = prog.launches.size();
+  cudaError_t err;
+  if (prog.nstreams <= 1) {
+    for (const Launch& L : prog.launches)
+      if ((err = run_launch(prog, L, bases, loss, st)) != cudaSuccess) return err;
+    return cudaSuccess;
+  }
+  auto strm = [&](int i) { return i == 0 ? st : prog.side[i - 1]; };
+  // fork: every side stream waits for the caller's work before the program
+  cudaEvent_t fork = prog.ev[nl];
+  if ((err = cudaEventRecord(fork, st)) != cudaSuccess) return err;
+  for (int i = 1; i < prog.nstreams; ++i)
+    if ((err = cudaStreamWaitEvent(strm(i), fork, 0)) != cudaSuccess) return err;
+  for (size_t k = 0; k < nl; ++k) {
+    const Launch& L = prog.launches[k];
+    cudaStream_t s = strm(L.stream);
+    for (int d : L.deps)
+      if (prog.launches[d].stream != L.stream)
+        if ((err = cudaStreamWaitEvent(s, prog.ev[d], 0)) != cudaSuccess) return err;
+    if ((err = run_launch(prog, L, bases, loss, s)) != cudaSuccess) return err;
+    if (L.signal && (err = cudaEventRecord(prog.ev[k], s)) != cudaSuccess) return err;
+  }
+  // join: the caller's stream waits for every side stream
+  for (int i = 1; i < prog.nstreams; ++i) {
+    cudaEvent_t j = prog.ev[nl + i];
+    if ((err = cudaEventRecord(j, strm(i))) != cudaSuccess) return err;
+    if ((err = cudaStreamWaitEvent(st, j, 0)) != cudaSuccess) return err;
   }
   return cudaSuccess;
 }
@@ -1197,6 +1253,7 @@ struct BatchPlan {
 };
 
 static const i64 kChunkElems = (i64)3 << 20;  // 24 MB of workspace per L2 chunk
+static const int kLanes = 2;                   // chunks in flight (48 MB of workspace in L2)
 
 static void build_batch_program(BatchPlan* B, float sign, Program& prog,
                                 std::vector<std::pair<i64, Program>>& fallback, bool cot) {
@@ -1276,32 +1333,60 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
       fallback.emplace_back(i, std::move(p));
     }
   }
-  for (auto& kv : single) {
-    // heavy items first
-    std::stable_sort(kv.second.items.begin(), kv.second.items.end(),
-                     [&](const WorkItem& a, const WorkItem& b) {
-                       return kv.second.descs[a.desc].slen > kv.second.descs[b.desc].slen;
-                     });
-    prog.launches.push_back(kv.second);
-  }
-  // multi-pass transforms: chunks by workspace size, one launch per pass index
-  std::sort(bigs.begin(), bigs.end(), [](const Big& a, const Big& b) { return a.mp.ws_total > b.mp.ws_total; });
+  // Streams: (lane, CTA size class).  Lanes kLanes are the chunk pipelines,
+  // lane kLanes holds the single-tile launches; classes are the CTA sizes
+  // 128, 256, 512.
+  auto cls_of = [](int threads) { return threads >= 512 ? 2 : (threads >= 256 ? 1 : 0); };
+  const int NC = 3;
   i64 peak = 0;
-  size_t k = 0;
-  while (k < bigs.size()) {
+  auto stream_of = [&](int lane, int threads) { return lane * NC + cls_of(threads); };
+  int max_stream = 0;
+  // the single-tile launches depend on nothing
+  for (auto it = single.rbegin(); it != single.rend(); ++it) {
+    Launch& L = it->second;
+    // heavy items first
+    std::stable_sort(L.items.begin(), L.items.end(), [&](const WorkItem& a, const WorkItem& b) {
+      return L.descs[a.desc].slen > L.descs[b.desc].slen;
+    });
+    L.stream = stream_of(kLanes, L.threads);
+    max_stream = std::max(max_stream, L.stream);
+    prog.launches.push_back(L);
+  }
+  // multi-pass transforms: chunks of at most kChunkElems of workspace; chunk
+  // c runs on lane c mod kLanes in that lane's workspace region, so kLanes
+  // chunks are in flight and each chunk's passes stay in L2.  Within a chunk,
+  // pass st of every transform waits for pass st-1 of the chunk; the first
+  // pass of a chunk waits for the last pass of the lane's previous chunk
+  // (workspace reuse).
+  std::sort(bigs.begin(), bigs.end(), [](const Big& a, const Big& b) { return a.mp.ws_total > b.mp.ws_total; });
+  std::vector<std::pair<size_t, size_t>> chunks;
+  i64 lane_ws = 0;
+  for (size_t k = 0; k < bigs.size();) {
     i64 used = 0;
     size_t e = k;
     while (e < bigs.size() && (e == k || used + bigs[e].mp.ws_total + 128 <= kChunkElems)) {
       used += (bigs[e].mp.ws_total + 63) / 64 * 64 + 64;
       ++e;
     }
+    chunks.emplace_back(k, e);
+    lane_ws = std::max(lane_ws, used);
+    k = e;
+  }
+  lane_ws = (lane_ws + 63) / 64 * 64;
+  std::vector<std::vector<int>> lane_last(kLanes);  // launches of the lane's previous chunk's last pass
+  for (size_t c = 0; c < chunks.size(); ++c) {
+    const size_t k = chunks[c].first, e = chunks[c].second;
+    const int lane = (int)(c % kLanes);
+    const i64 ws0 = lane * lane_ws;
     size_t maxsteps = 0;
     for (size_t j = k; j < e; ++j) maxsteps = std::max(maxsteps, bigs[j].mp.steps.size());
+    std::vector<int> prev = lane_last[lane];
     for (size_t st = 0; st < maxsteps; ++st) {
-      Launch L;
-      L.type = L_TILE;
-      std::map<std::pair<i64, int>, int> dmap;
-      i64 wpos = 0;
+      // one launch per CTA size: a few large tiles do not hold the many
+      // small ones to their shared-memory footprint
+      std::map<int, Launch> cls;
+      std::map<int, std::map<std::pair<i64, int>, int>> dmaps;
+      i64 wpos = ws0;
       for (size_t j = k; j < e; ++j) {
         const Big& b = bigs[j];
         const i64 woff = wpos;
@@ -1309,6 +1394,9 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
         if (st >= b.mp.steps.size()) continue;
         const TileStep& s = b.mp.steps[st];
         const i64 n = B->ns[b.i];
+        Launch& L = cls[s.threads];
+        L.type = L_TILE;
+        auto& dmap = dmaps[s.threads];
         auto key = std::make_pair(n, s.threads);
         int di;
         auto it = dmap.find(key);
@@ -1324,12 +1412,26 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
         const i64 out_add = s.d.out.buf == BUF_WS ? woff : B->offs[b.i];
         append_tile(L, s, di, in_add, out_add);
       }
-      if (!L.items.empty()) prog.launches.push_back(L);
+      std::vector<int> cur;
+      // largest CTAs first: their few long CTAs start before the many short ones
+      for (auto it = cls.rbegin(); it != cls.rend(); ++it) {
+        Launch& L = it->second;
+        if (L.items.empty()) continue;
+        L.stream = stream_of(lane, L.threads);
+        max_stream = std::max(max_stream, L.stream);
+        L.deps = prev;
+        for (int d : prev)
+          if (prog.launches[d].stream != L.stream) prog.launches[d].signal = true;
+        cur.push_back((int)prog.launches.size());
+        prog.launches.push_back(L);
+      }
+      prev = cur;
       peak = std::max(peak, wpos);
     }
-    k = e;
+    lane_last[lane] = prev;
   }
   prog.ws_elems = peak;
+  prog.nstreams = max_stream + 1;
   finalize_program(B->res, prog);
 }
 

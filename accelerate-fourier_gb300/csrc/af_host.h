@@ -48,11 +48,20 @@ struct Launch {
   int g_max = 0;
   MapDesc md;
   size_t desc_off = 0, item_off = 0;  // byte offsets in the program's device blob
+  // Concurrent execution (batched programs): the launch runs on side stream
+  // `stream` (0 = the caller's) after the launches listed in `deps`
+  // (indices into the program); launches on one stream run in program order.
+  int stream = 0;
+  std::vector<int> deps;
+  bool signal = false;  // a launch on another stream depends on this one
 };
 
 struct Program {
   std::vector<Launch> launches;
   i64 ws_elems = 0;
+  int nstreams = 1;                // streams the launches use (1: sequential)
+  std::vector<cudaStream_t> side;  // streams 1 .. nstreams-1
+  std::vector<cudaEvent_t> ev;     // per launch (signalling launches), then fork and joins
   char* dblob = nullptr;  // device copy of every launch's descriptors and items
   int tile_launches() const;
 };
@@ -94,6 +103,8 @@ struct PlanRes {
   std::map<std::pair<i64, i64>, const float2*> pair_tables;
   std::map<std::pair<i64, int>, RaderRes> rader;
   std::map<std::tuple<i64, i64, int>, ChirpRes> chirps;
+  std::vector<cudaStream_t> streams;  // owned side streams of programs
+  std::vector<cudaEvent_t> events;
   void* dalloc(size_t bytes);
   TwTable table(i64 n);
   const float2* pair_table(i64 a, i64 b, int* off_b);

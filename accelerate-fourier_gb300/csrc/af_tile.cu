@@ -31,25 +31,25 @@ struct PhaseRegs {
 };
 
 
-// u[j] *= w1^j for j = 1..R-1.  The powers are built as w^(Q a + b) =
-// (w^Q)^a * w^b from the small powers w^b (b < Q) and w^Q, so that at most a
-// handful of complex values are live and no power is more than five
-// products deep.
+// u[j] *= w^j for j = 1..R-1 with w = W^t1 from the phase table.  The
+// powers are w^(Q a + b) = W^(Q a t1) * w^b: the W^(Q a t1) come from the
+// table, the small powers w^b (b < Q <= 4) from at most two products, so
+// every twiddle is within three rounded products of table values.
 template <int R>
-__device__ __forceinline__ void apply_twiddles(float2* u, float2 w1) {
+__device__ __forceinline__ void apply_twiddles(float2* u, const float2* __restrict__ ptab, int S_log2, int t1,
+                                               float sign) {
   constexpr int Q = R <= 4 ? 2 : (R <= 9 ? 3 : 4);
   float2 s[Q];
   s[0] = make_float2(1.f, 0.f);
-  s[1] = w1;
+  s[1] = tw_lookup(ptab, S_log2, t1, sign);
 #pragma unroll
-  for (int b = 2; b < Q; ++b) s[b] = b == 2 ? cmul(w1, w1) : cmul(s[b - 1], w1);
-  const float2 big = Q == 2 ? cmul(w1, w1) : (Q == 4 ? cmul(s[2], s[2]) : cmul(s[2], w1));  // w^Q
-  float2 base = big;
+  for (int b = 2; b < Q; ++b) s[b] = b == 2 ? cmul(s[1], s[1]) : cmul(s[2], s[1]);
+  float2 big = s[0];
 #pragma unroll
   for (int j = 1; j < R; ++j) {
     const int a = j / Q, b = j % Q;
-    if (a >= 2 && b == 0) base = a == 2 ? cmul(big, big) : cmul(base, big);
-    const float2 w = a == 0 ? s[b] : (b == 0 ? base : cmul(base, s[b]));
+    if (a >= 1 && b == 0) big = tw_lookup(ptab, S_log2, j * t1, sign);
+    const float2 w = a == 0 ? s[b] : (b == 0 ? big : cmul(big, s[b]));
     u[j] = cmul(u[j], w);
   }
 }
@@ -78,7 +78,7 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
     for (int j = 0; j < R; ++j) u[j] = src[spad(ib + j * nbe)];
     const int q = (int)fdiv((unsigned)i, pdv);
     const int k = i - q * p;
-    if (k > 0) apply_twiddles<R>(u, tw_lookup(ptab, ph.S_log2, k * tws, ph.sign));
+    if (k > 0) apply_twiddles<R>(u, ptab, ph.S_log2, k * tws, ph.sign);
     Dft<R>::run(u, ph.sign, ptab, ph.S_log2, ph.n);
     const int ob = base + (q * p * R + k) * ph.es;
 #pragma unroll

@@ -111,7 +111,7 @@ def test_benchmark_workload_sample():
     import bench
     sizes = bench.workload_sizes()
     b = make_batch(sizes, -1)
-    assert b.launches() <= 64
+    assert b.launches() <= 160
     rng = np.random.default_rng(5)
     x = crand(rng, int(sizes.sum()), "normal")
     y = run(b, x)
