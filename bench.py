@@ -34,6 +34,7 @@ for _p in (ROOT, os.path.join(ROOT, "accelerate-fourier_gb300")):
 METRIC = "C2C FFT GB/s & % HBM roofline (fwd+VJP, batched mixed N) vs plain; err vs FP64"
 UNIT = "GB/s"
 COUNT = 4096
+STEP_DRAM_BYTES = 2.652e9  # DRAM bytes per step of the default workload (ncu, see the profiles)
 
 
 # ----------------------------------------------------------------- workload
@@ -361,6 +362,10 @@ def run_ours(args):
     # algorithmic bytes per step: read x, read w, write g, read g, write grad
     alg_bytes = total * (8 + 4 + 8 + 8 + 8)
     achieved = alg_bytes / (ms * 1e-3) / 1e9
+    # DRAM bytes of one step's tile-kernel launches (dram__bytes_read.sum +
+    # dram__bytes_write.sum from an ncu launch list of this workload with L2
+    # kept between launches); measured, not derived
+    traffic = STEP_DRAM_BYTES if args.count == COUNT else None
     cpu = None
     if not args.no_cpu and world == 1:
         v, cores, sample = cpu_baseline(ns)
@@ -380,9 +385,10 @@ def run_ours(args):
         "e2e": {"value": world * nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(xh.nbytes + wh.nbytes), "d2h_bytes_per_step": int(xh.nbytes + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": traffic,
                      "note": "tile kernel over the whole step: algorithmic 36 B per point "
-                             "(x, w, g, g, grad) / step time; peak = measured copy bandwidth"},
+                             "(x, w, g, g, grad) / step time; peak = measured copy bandwidth; "
+                             "traffic = DRAM bytes per step (ncu)"},
         "cpu_baseline": cpu,
         "gpu_launches": runner.launches_per_step * args.steps * world,
         "clocks": clk,
