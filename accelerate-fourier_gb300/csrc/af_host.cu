@@ -391,7 +391,9 @@ static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, i
   if (!fits(g)) throw AfError(AF_ERR_UNSUPPORTED, "transform does not fit a tile");
   *G = (int)g;
   const i64 elems = g * slen;
-  *threads = elems > 8192 ? 512 : (elems >= 1024 ? 256 : 128);
+  // CTAs of up to 4096 elements (two buffers, 83 KB) fit two per SM; larger
+  // tiles take 512 threads and a whole SM
+  *threads = elems > 4096 ? 512 : (elems >= 1024 ? 256 : 128);
 }
 
 struct TileStep {
@@ -899,7 +901,19 @@ static void make_program_streams(PlanRes& res, Program& prog) {
   }
 }
 
+// A one-phase PLAIN tile with AFFINE views and no Rader capture: the
+// specialised (smaller) kernel runs it.
+static bool simple_desc(const TileDesc& d) {
+  return d.kind == TILE_PLAIN && d.in.map == IO_AFFINE && d.out.map == IO_AFFINE && d.nph == 1 && d.x0_cap < 0;
+}
+
 void finalize_program(PlanRes& res, Program& prog) {
+  for (Launch& L : prog.launches) {
+    if (L.type != L_TILE) continue;
+    L.generic = 0;
+    for (const TileDesc& d : L.descs)
+      if (!simple_desc(d)) L.generic = 1;
+  }
   make_program_streams(res, prog);
   size_t bytes = 0;
   for (Launch& L : prog.launches) {
@@ -959,6 +973,7 @@ static cudaError_t run_launch(const Program& prog, const Launch& L, const TileBa
     spec.threads = L.threads;
     spec.smem_data = L.smem_data;
     spec.smem_bytes = tile_smem_bytes(L.smem_data, kMaxTw, kMaxG);
+    spec.generic = L.generic;
     return launch_tiles(spec, bases, loss, st);
   }
   return launch_map(L.md, bases, st);
@@ -1263,12 +1278,12 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   // stage 0: single-tile transforms, one launch per thread class
   // single-tile launches are split by CTA size and shared-memory class, so
   // that small transforms are not held to the occupancy of large ones
-  std::map<std::pair<int, int>, Launch> single;
+  std::map<std::pair<int, int>, Launch> single;  // (threads * 2 + simple, smem class)
   std::map<std::pair<i64, int>, int> single_desc;  // (n, threads) -> desc index
   auto single_key = [](const TileStep& s) {
     int c = 0;
     while ((1 << c) < spad_host(s.d.G * s.d.LS) + 2) ++c;
-    return std::make_pair(s.threads, c);
+    return std::make_pair(s.threads * 2 + (simple_desc(s.d) ? 1 : 0), c);
   };
   struct Big {
     i64 i;
@@ -1336,10 +1351,11 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   // Streams: (lane, CTA size class).  Lanes kLanes are the chunk pipelines,
   // lane kLanes holds the single-tile launches; classes are the CTA sizes
   // 128, 256, 512.
-  auto cls_of = [](int threads) { return threads >= 512 ? 2 : (threads >= 256 ? 1 : 0); };
-  const int NC = 3;
+  // classes: CTA size x (specialised or general kernel)
+  auto cls_of = [](int threads, bool simple) { return (threads >= 512 ? 2 : (threads >= 256 ? 1 : 0)) * 2 + simple; };
+  const int NC = 6;
   i64 peak = 0;
-  auto stream_of = [&](int lane, int threads) { return lane * NC + cls_of(threads); };
+  auto stream_of = [&](int lane, int threads, bool simple) { return lane * NC + cls_of(threads, simple); };
   int max_stream = 0;
   // the single-tile launches depend on nothing
   for (auto it = single.rbegin(); it != single.rend(); ++it) {
@@ -1348,7 +1364,9 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     std::stable_sort(L.items.begin(), L.items.end(), [&](const WorkItem& a, const WorkItem& b) {
       return L.descs[a.desc].slen > L.descs[b.desc].slen;
     });
-    L.stream = stream_of(kLanes, L.threads);
+    bool simple = true;
+    for (const TileDesc& d : L.descs) simple = simple && simple_desc(d);
+    L.stream = stream_of(kLanes, L.threads, simple);
     max_stream = std::max(max_stream, L.stream);
     prog.launches.push_back(L);
   }
@@ -1384,7 +1402,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     for (size_t st = 0; st < maxsteps; ++st) {
       // one launch per CTA size: a few large tiles do not hold the many
       // small ones to their shared-memory footprint
-      std::map<int, Launch> cls;
+      std::map<int, Launch> cls;  // threads * 2 + simple
       std::map<int, std::map<std::pair<i64, int>, int>> dmaps;
       i64 wpos = ws0;
       for (size_t j = k; j < e; ++j) {
@@ -1394,9 +1412,10 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
         if (st >= b.mp.steps.size()) continue;
         const TileStep& s = b.mp.steps[st];
         const i64 n = B->ns[b.i];
-        Launch& L = cls[s.threads];
+        const int ck = s.threads * 2 + (simple_desc(s.d) ? 1 : 0);
+        Launch& L = cls[ck];
         L.type = L_TILE;
-        auto& dmap = dmaps[s.threads];
+        auto& dmap = dmaps[ck];
         auto key = std::make_pair(n, s.threads);
         int di;
         auto it = dmap.find(key);
@@ -1417,7 +1436,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
       for (auto it = cls.rbegin(); it != cls.rend(); ++it) {
         Launch& L = it->second;
         if (L.items.empty()) continue;
-        L.stream = stream_of(lane, L.threads);
+        L.stream = stream_of(lane, L.threads, (it->first & 1) != 0);
         max_stream = std::max(max_stream, L.stream);
         L.deps = prev;
         for (int d : prev)

@@ -52,6 +52,7 @@ struct Launch {
   // `stream` (0 = the caller's) after the launches listed in `deps`
   // (indices into the program); launches on one stream run in program order.
   int stream = 0;
+  int generic = 1;  // tile launch needs the general kernel (not only PLAIN tiles with AFFINE views)
   std::vector<int> deps;
   bool signal = false;  // a launch on another stream depends on this one
 };

@@ -16,6 +16,7 @@ struct LaunchSpec {
   int nitems;
   int threads;
   int smem_data;      // float2 per ping-pong buffer (max over the launch's descriptors)
+  int generic;        // 0: every descriptor is a one-phase PLAIN tile with AFFINE views
   size_t smem_bytes;  // dynamic shared memory of the launch
 };
 size_t tile_smem_bytes(int smem_data, int tw_total, int G);

@@ -279,7 +279,10 @@ __device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, float2
   gst(*sc.B, buf, a, v);
 }
 
-template <int T>
+// GEN = false compiles only PLAIN tiles with AFFINE views, one phase and no
+// Rader captures (most tiles): a much smaller kernel, kinder to the
+// instruction cache.
+template <int T, bool GEN>
 __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it, const TileBases& B,
                                           float2* A, float2* Bf, const float2* tab, float2* xs, double* loss) {
   const int line0 = it.line0;
@@ -302,7 +305,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   // Per-line base offsets of AFFINE views (hi*s_hi + lo*s_lo, relative to
   // the view's offset) for the CTA's G lines, input then output; PLAIN and
   // CONVROW tiles keep them in the per-line scratch (16 bytes per line).
-  const bool rows_kind = d.kind == TILE_PLAIN || d.kind == TILE_CONVROW;
+  const bool rows_kind = !GEN || d.kind == TILE_PLAIN || d.kind == TILE_CONVROW;
   i64* lbi = reinterpret_cast<i64*>(xs);
   i64* lbo = lbi + G;
   if (rows_kind) {
@@ -324,7 +327,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   if (rows_kind) {
     const IoRegs r = io_regs(in, B, ibase);
     const int lf = in.line_fast;
-    switch (in.map) {
+    switch (GEN ? in.map : (int)IO_AFFINE) {
       case IO_AFFINE:
         if (r.s_e == 1) {
           load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
@@ -368,7 +371,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         }, sm);
         break;
     }
-    if (d.x0_cap >= 0 && threadIdx.x == 0) {
+    if (GEN && d.x0_cap >= 0 && threadIdx.x == 0) {
       for (int l = 0; l < G; ++l) {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
@@ -418,7 +421,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
 
   // ------------------------------------------------------------ phases
   sm = run_phase<T>(A, Bf, &d.ph[0], d.LS, G, tab);
-  if (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN || d.kind == TILE_CONVROW) {
+  if (GEN && (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN || d.kind == TILE_CONVROW)) {
     // FFT(+1) -> * spectrum -> FFT(-1): the direction order of the reference's
     // convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
     if (d.kind == TILE_RADER) {
@@ -449,7 +452,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     }
     __syncthreads();
   }
-  if (d.nph > 1) sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[1], d.LS, G, tab);
+  if (GEN && d.nph > 1) sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[1], d.LS, G, tab);
 
   // ------------------------------------------------------------ store
   StoreCtx sc{&B, 0.f, d.cot};
@@ -462,7 +465,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     const float scale = d.scale;
     const int cot = d.cot;
     const float* __restrict__ wp = B.c[BUF_AUX] ? reinterpret_cast<const float*>(B.c[BUF_AUX]) : B.re[BUF_AUX];
-    const int omap = out.map;
+    const int omap = GEN ? out.map : (int)IO_AFFINE;
     // Rader scatter: x0 of transform hi and the DC slot
     const float2* x0p = B.c[out.x0_buf] + out.x0_off + (out.x0_buf == in.buf ? it.in_add : it.out_add);
     const i64 x0_shi = out.x0_shi;
@@ -556,7 +559,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   }
 }
 
-template <int T>
+template <int T, bool GEN>
 __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const TileDesc* __restrict__ descs,
                                                  const WorkItem* __restrict__ items, TileBases bases,
                                                  double* loss, int smem_data) {
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
   float2* tab = Bf + smem_data;
   float2* xs = tab + d->tw_total;
   for (int i = threadIdx.x; i < d->tw_total; i += T) tab[i] = d->tw_src[i];
-  tile_body<T>(*d, it, bases, A, Bf, tab, xs, loss);
+  tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
 size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
@@ -587,7 +590,7 @@ size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
 
 // Raises the kernel's dynamic shared-memory limit to what the device allows
 // once per process (the opt-in limit less the kernel's static usage).
-template <int T>
+template <int T, bool GEN>
 static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
   static int limit = -1;
   if (limit < 0) {
@@ -595,9 +598,9 @@ static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double*
     cudaFuncAttributes fa;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, tile_kernel<T>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, tile_kernel<T, GEN>);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(tile_kernel<T, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                optin - (int)fa.sharedSizeBytes);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -606,16 +609,23 @@ static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double*
     limit = optin - (int)fa.sharedSizeBytes;
   }
   if (L.smem_bytes > (size_t)limit) return cudaErrorInvalidValue;
-  tile_kernel<T><<<L.nitems, T, L.smem_bytes, st>>>(L.descs, L.items, bases, loss, L.smem_data);
+  tile_kernel<T, GEN><<<L.nitems, T, L.smem_bytes, st>>>(L.descs, L.items, bases, loss, L.smem_data);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tiles(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
   if (L.nitems <= 0) return cudaSuccess;
+  if (L.generic) {
+    switch (L.threads) {
+      case 512: return launch_t<512, true>(L, bases, loss, st);
+      case 128: return launch_t<128, true>(L, bases, loss, st);
+      default: return launch_t<256, true>(L, bases, loss, st);
+    }
+  }
   switch (L.threads) {
-    case 512: return launch_t<512>(L, bases, loss, st);
-    case 128: return launch_t<128>(L, bases, loss, st);
-    default: return launch_t<256>(L, bases, loss, st);
+    case 512: return launch_t<512, false>(L, bases, loss, st);
+    case 128: return launch_t<128, false>(L, bases, loss, st);
+    default: return launch_t<256, false>(L, bases, loss, st);
   }
 }
 
