@@ -159,3 +159,24 @@ def test_cyclic_reverse_and_scale_exact():
     assert np.array_equal(y, O().cyclic_reverse(x.astype(np.complex128)).astype(np.complex64))
     s = to_host(utility.scaleDown(to_dev(x)))
     assert np.allclose(s, x / 37, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("n", [1 << 20, 3 ** 12, 1001 * 1024, 65537, 1000003])
+def test_config2_single_transforms(n):
+    """Batch 1, re/im i.i.d. N(0,1), seed 2: 2^20, 3^12, 1001*1024, 65537
+    (Rader), 1000003 (the planner picks Bluestein, pad 2025000).  Bound:
+    rel-L2 <= 4 eps32 log2 N against the FP64 oracle; max-abs error <= 8 eps32
+    log2 N times the largest output magnitude."""
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(2)
+    x = crand(rng, (1, n), "normal")
+    t = planned.transform(-1, n)
+    if n == 1000003:
+        assert t.describe().startswith("BL1000003")
+    y = to_host(t(to_dev(x)))
+    ref = O().planned(x, -1)
+    # the oracle's Bluestein computes the chirp phase pi k^2/N in FP64 as the
+    # reference does (k^2 up to 1e12): about 2e-10 from numpy at N = 1000003
+    assert rel_l2(ref, np.fft.fft(x, axis=-1)) <= (1e-9 if n == 1000003 else 1e-12)
+    assert rel_l2(y, ref) <= fp32_bound(n, 4.0)
+    assert np.abs(y - ref).max() <= 8 * 2.0 ** -24 * np.log2(n) * np.abs(ref).max()
