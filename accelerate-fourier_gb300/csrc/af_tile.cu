@@ -214,6 +214,36 @@ __device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, con
   }
 }
 
+// Asynchronous copy of G lines x N interleaved elements into shared memory
+// (cp.async, 8 bytes per element): `src(l, e)` gives the global address of
+// element e of line l.  No register staging: every element of the tile is in
+// flight at once.  The caller's barrier follows the wait.
+__device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+template <int T, class F>
+__device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndiv, const FastDiv& Gdiv,
+                                                int line_fast, int LS, F src, float2* sm) {
+  const int tot = G * N;
+  for (int q = threadIdx.x; q < tot; q += T) {
+    int l, e;
+    if (!line_fast) {
+      l = (int)fdiv((unsigned)q, Ndiv);
+      e = q - l * N;
+    } else {
+      e = (int)fdiv((unsigned)q, Gdiv);
+      l = q - e * G;
+    }
+    cp_async8(sm + spad(l * LS + e), src(l, e));
+  }
+  cp_async_wait_all();
+}
+
 // A global view (IoDesc) copied into registers with its base pointer resolved.
 struct IoRegs {
   float2* c;
@@ -329,7 +359,15 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     const int lf = in.line_fast;
     switch (GEN ? in.map : (int)IO_AFFINE) {
       case IO_AFFINE:
-        if (r.s_e == 1) {
+        if (r.c) {  // interleaved: asynchronous copies straight into shared memory
+          const float2* c = r.c;
+          const i64 se = r.s_e;
+          if (se == 1)
+            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e) { return c + lbi[l] + e; }, sm);
+          else
+            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS,
+                               [&](int l, int e) { return c + lbi[l] + (i64)e * se; }, sm);
+        } else if (r.s_e == 1) {
           load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
             v = rld(r, lbi[l] + e);
             return spad(l * LS + e);
