@@ -216,7 +216,7 @@ __device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, con
 
 // Asynchronous copy of G lines x N interleaved elements into shared memory
 // (cp.async, 8 bytes per element): `src(l, e)` gives the global address of
-// element e of line l.  No register staging: every element of the tile is in
+// element e of line l, or nullptr for a zero.  No register staging: every element of the tile is in
 // flight at once.  The caller's barrier follows the wait.
 __device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
@@ -239,7 +239,11 @@ __device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndi
       e = (int)fdiv((unsigned)q, Gdiv);
       l = q - e * G;
     }
-    cp_async8(sm + spad(l * LS + e), src(l, e));
+    int pos = spad(l * LS + e);  // src may move the element (permuted tiles)
+    const float2* g = src(l, e, pos);
+    float2* d = sm + pos;
+    if (g) cp_async8(d, g);
+    else *d = make_float2(0.f, 0.f);  // zero padding
   }
   cp_async_wait_all();
 }
@@ -363,10 +367,10 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           const float2* c = r.c;
           const i64 se = r.s_e;
           if (se == 1)
-            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e) { return c + lbi[l] + e; }, sm);
+            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) { return c + lbi[l] + e; }, sm);
           else
             load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS,
-                               [&](int l, int e) { return c + lbi[l] + (i64)e * se; }, sm);
+                               [&](int l, int e, int&) { return c + lbi[l] + (i64)e * se; }, sm);
         } else if (r.s_e == 1) {
           load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
             v = rld(r, lbi[l] + e);
@@ -381,6 +385,15 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         }
         break;
       case IO_GT:
+        if (r.c) {
+          const float2* c = r.c;
+          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) {
+            int hi, lo;
+            rsplit(r, line0 + l, hi, lo);
+            return c + (i64)hi * r.s_hi + (i64)rgt(r, lo, e) * r.s_t;
+          }, sm);
+          break;
+        }
         load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
@@ -389,6 +402,17 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         }, sm);
         break;
       case IO_TABLE:  // zero beyond the table length mN
+        if (r.c) {
+          const float2* c = r.c;
+          const float2* zero = nullptr;
+          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) {
+            int hi, lo;
+            rsplit(r, line0 + l, hi, lo);
+            const i64 q = lo * r.q_lo + e * r.q_e;
+            return q < r.mN ? c + (i64)hi * r.s_hi + (i64)__ldg(&r.tab[q]) * r.s_t : zero;
+          }, sm);
+          break;
+        }
         load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
@@ -419,14 +443,26 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   } else if (d.kind == TILE_GT) {
     // grid position (k, j) holds x[(n k + m j) mod N]  (Planned.hs:597-606);
     // inverting: k = i*cm mod m, j = i*cn mod n
-    load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
-      int hi, lo;
-      split_line(in, line0 + l, hi, lo);
-      const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
-      const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
-      v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, i));
-      return spad(l * d.LS + k * d.gt_n + j);
-    }, sm);
+    if (B.c[in.buf]) {
+      const float2* c = B.c[in.buf];
+      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, [&](int l, int i, int& pos) {
+        int hi, lo;
+        split_line(in, line0 + l, hi, lo);
+        const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
+        const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
+        pos = spad(l * d.LS + k * d.gt_n + j);
+        return c + io_addr(in, ibase, hi, lo, i);
+      }, sm);
+    } else {
+      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
+        int hi, lo;
+        split_line(in, line0 + l, hi, lo);
+        const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
+        const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
+        v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, i));
+        return spad(l * d.LS + k * d.gt_n + j);
+      }, sm);
+    }
   } else if (d.kind == TILE_RADER) {
     // a[q] = x[g^-q]  (Permutation.apply rev res, Planned.hs:686-692): input
     // index r >= 1 with g^dlog(r) = r goes to q = (-dlog r) mod (p-1)
@@ -437,14 +473,29 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       sm[spad(l * d.LS + m + (q - l * (d.slen - m)))] = make_float2(0.f, 0.f);
     }
     const int xs_pos = (int)(xs - sm);  // x0 of line l goes to xs[2 l]
-    load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, float2& v) -> int {
-      int hi, lo;
-      split_line(in, line0 + l, hi, lo);
-      v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, r));
-      if (r == 0) return xs_pos + 2 * l;
-      const int lg = __ldg(&d.dlog[r - 1]);
-      return spad(l * d.LS + (lg == 0 ? 0 : m - lg));
-    }, sm);
+    if (B.c[in.buf]) {
+      const float2* c = B.c[in.buf];
+      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, [&](int l, int r, int& pos) {
+        int hi, lo;
+        split_line(in, line0 + l, hi, lo);
+        if (r == 0) {
+          pos = xs_pos + 2 * l;
+        } else {
+          const int lg = __ldg(&d.dlog[r - 1]);
+          pos = spad(l * d.LS + (lg == 0 ? 0 : m - lg));
+        }
+        return c + io_addr(in, ibase, hi, lo, r);
+      }, sm);
+    } else {
+      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, float2& v) -> int {
+        int hi, lo;
+        split_line(in, line0 + l, hi, lo);
+        v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, r));
+        if (r == 0) return xs_pos + 2 * l;
+        const int lg = __ldg(&d.dlog[r - 1]);
+        return spad(l * d.LS + (lg == 0 ? 0 : m - lg));
+      }, sm);
+    }
   } else {  // TILE_BLUESTEIN: chirp * x zero padded to M (Planned.hs:765-773)
     const int M = d.slen;
     load_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e, float2& v) -> int {
