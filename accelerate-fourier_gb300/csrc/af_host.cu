@@ -152,11 +152,15 @@ static std::vector<float2> to_f32(const std::vector<cd>& v) {
 // p-1 itself when it is 13-smooth (the reference's Rader), otherwise the
 // least 13-smooth M >= 2(p-1)-1, so that the cyclic convolution of length p-1
 // runs as one zero-padded convolution instead of nested Rader transforms.
+// Length of the transforms that carry Rader's cyclic convolution of p-1:
+// p-1 itself when it is 13-smooth, else the least 5-smooth M >= 2(p-1)-1
+// (zero padding; 5-smooth lengths avoid the costlier radix-7/11/13 passes
+// for a few percent more elements).
 i64 rader_conv_len(i64 p) {
   const i64 m = p - 1;
   if (is_13smooth(m)) return m;
   i64 M = 2 * m - 1;
-  while (!is_13smooth(M)) ++M;
+  while (!is_5smooth(M)) ++M;
   return M;
 }
 
@@ -1327,7 +1331,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     // no fused scheme for this plan tree: the DFT of length n runs as one
     // zero-padded Bluestein convolution (chirp-z) of 13-smooth length
     i64 pad = 2 * n - 1;
-    while (!is_13smooth(pad)) ++pad;
+    while (!is_5smooth(pad)) ++pad;
     const Node* ch = B->planner.chirp(n, pad);
     if (single_tile_ok(ch)) {
       TileStep s = single_step(B->res, ch, sign, 1, in, out);
