@@ -509,39 +509,42 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   __syncthreads();
 
   // ------------------------------------------------------------ phases
-  sm = run_phase<T>(A, Bf, &d.ph[0], d.LS, G, tab);
-  if (GEN && (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN || d.kind == TILE_CONVROW)) {
-    // FFT(+1) -> * spectrum -> FFT(-1): the direction order of the reference's
-    // convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
-    if (d.kind == TILE_RADER) {
-      for (int l = threadIdx.x; l < G; l += T) xs[2 * l + 1] = sm[spad(l * d.LS)];  // sum res
-      __syncthreads();
-    }
-    const int M = d.slen;
-    if (d.kind == TILE_CONVROW) {
-      if (d.dc_off >= 0 && threadIdx.x == 0) {
-        for (int l = 0; l < G; ++l) {
+  // One inlined copy of the passes serves both phases (half the code of two).
+  const int nph = GEN ? d.nph : 1;
+  for (int phi = 0; phi < nph; ++phi) {
+    if (GEN && phi == 1 && (d.kind == TILE_RADER || d.kind == TILE_BLUESTEIN || d.kind == TILE_CONVROW)) {
+      // FFT(+1) -> * spectrum -> FFT(-1): the direction order of the reference's
+      // convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
+      if (d.kind == TILE_RADER) {
+        for (int l = threadIdx.x; l < G; l += T) xs[2 * l + 1] = sm[spad(l * d.LS)];  // sum res
+        __syncthreads();
+      }
+      const int M = d.slen;
+      if (d.kind == TILE_CONVROW) {
+        if (d.dc_off >= 0 && threadIdx.x == 0) {
+          for (int l = 0; l < G; ++l) {
+            int hi, lo;
+            split_line(out, line0 + l, hi, lo);
+            if (lo == 0) B.c[BUF_WS][d.dc_off + it.out_add + hi] = sm[spad(l * d.LS)];
+          }
+        }
+        __syncthreads();
+        for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
           int hi, lo;
           split_line(out, line0 + l, hi, lo);
-          if (lo == 0) B.c[BUF_WS][d.dc_off + it.out_add + hi] = sm[spad(l * d.LS)];
-        }
+          const int a = spad(l * d.LS + e);
+          sm[a] = cmul(__ldg(&d.vec_b[lo * d.sq_lo + e * d.sq_e]), sm[a]);
+        });
+      } else {
+        for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
+          const int a = spad(l * d.LS + e);
+          sm[a] = cmul(__ldg(&d.vec_b[e]), sm[a]);
+        });
       }
       __syncthreads();
-      for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
-        int hi, lo;
-        split_line(out, line0 + l, hi, lo);
-        const int a = spad(l * d.LS + e);
-        sm[a] = cmul(__ldg(&d.vec_b[lo * d.sq_lo + e * d.sq_e]), sm[a]);
-      });
-    } else {
-      for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
-        const int a = spad(l * d.LS + e);
-        sm[a] = cmul(__ldg(&d.vec_b[e]), sm[a]);
-      });
     }
-    __syncthreads();
+    sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[phi], d.LS, G, tab);
   }
-  if (GEN && d.nph > 1) sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[1], d.LS, G, tab);
 
   // ------------------------------------------------------------ store
   StoreCtx sc{&B, 0.f, d.cot};
