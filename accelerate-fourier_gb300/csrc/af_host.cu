@@ -976,7 +976,10 @@ static cudaError_t run_launch(const Program& prog, const Launch& L, const TileBa
     spec.nitems = (int)L.items.size();
     spec.threads = L.threads;
     spec.smem_data = L.smem_data;
-    spec.smem_bytes = tile_smem_bytes(L.smem_data, kMaxTw, kMaxG);
+    // shared memory for this launch's largest buffers, tables and line count:
+    // every tile fits the fixed allowances (choose_geometry), so the launch's
+    // maxima fit too, and small tiles keep more CTAs per SM
+    spec.smem_bytes = tile_smem_bytes(L.smem_data, L.tw_max, L.g_max);
     spec.generic = L.generic;
     return launch_tiles(spec, bases, loss, st);
   }

@@ -676,8 +676,11 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
   tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
+// descriptor, two buffers, tables, per-line scratch (at least 8 float2: the
+// loss reduction keeps one float per warp there)
 size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
-  return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + 2 * G) * sizeof(float2);
+  const int scratch = 2 * G > 8 ? 2 * G : 8;
+  return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + scratch) * sizeof(float2);
 }
 
 // Raises the kernel's dynamic shared-memory limit to what the device allows
