@@ -506,6 +506,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       return spad(l * d.LS + e);
     }, sm);
   }
+  cp_async_wait_all();  // tables (and any tile copies not yet waited for)
   __syncthreads();
 
   // ------------------------------------------------------------ phases
@@ -672,7 +673,9 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
   float2* Bf = A + smem_data;
   float2* tab = Bf + smem_data;
   float2* xs = tab + d->tw_total;
-  for (int i = threadIdx.x; i < d->tw_total; i += T) tab[i] = d->tw_src[i];
+  // the twiddle tables travel with the tile's own asynchronous copies (one
+  // wait for both, before the first pass)
+  for (int i = threadIdx.x; i < d->tw_total; i += T) cp_async8(tab + i, d->tw_src + i);
   tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
