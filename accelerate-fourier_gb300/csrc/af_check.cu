@@ -56,8 +56,16 @@ struct Checker {
     hi = line / d;
     lo = line - hi * d;
   }
-  static i64 addr(const IoDesc& io, i64 base, i64 hi, i64 lo, i64 e) {
+  i64 loff(const IoDesc& io, i64 line) {
+    auto it = res.host_loffs.find(io.loff);
+    if (it == res.host_loffs.end()) { fail("unknown line table"); return 0; }
+    if (line < 0 || line >= (i64)it->second.size()) { fail("line table read out of bounds"); return 0; }
+    return it->second[line];
+  }
+  // element e of line `line` (split into hi, lo) of an AFFINE or GT view
+  i64 addr(const IoDesc& io, i64 base, i64 line, i64 hi, i64 lo, i64 e) {
     if (io.map == IO_GT) return base + hi * io.s_hi + ((io.mA * lo + io.mB * e) % io.mN) * io.s_t;
+    if (io.loff) return base + loff(io, line) + e * io.s_e;
     return base + hi * io.s_hi + lo * io.s_lo + e * io.s_e;
   }
 
@@ -87,7 +95,7 @@ struct Checker {
       // ---- loads
       if (d.kind == TILE_PLAIN || d.kind == TILE_CONVROW) {
         for (i64 e = 0; e < N; ++e) {
-          if (in.map == IO_AFFINE || in.map == IO_GT) rd(in.buf, addr(in, ib, hi, lo, e));
+          if (in.map == IO_AFFINE || in.map == IO_GT) rd(in.buf, addr(in, ib, it.line0 + l, hi, lo, e));
           else if (in.map == IO_TABLE) {
             const i64 q = lo * in.q_lo + e * in.q_e;
             if (q < in.mN) rd(in.buf, ib + hi * in.s_hi + (i64)tab(in.tab, q) * in.s_t);
@@ -100,10 +108,8 @@ struct Checker {
           rd(in.buf, ib + hi * in.s_hi);
           wr(BUF_WS, d.x0_cap + it.out_add + hi);
         }
-      } else if (d.kind == TILE_BLUESTEIN) {
-        for (i64 e = 0; e < N; ++e) rd(in.buf, addr(in, ib, hi, lo, e));
       } else {
-        for (i64 e = 0; e < N; ++e) rd(in.buf, addr(in, ib, hi, lo, e));
+        for (i64 e = 0; e < N; ++e) rd(in.buf, addr(in, ib, it.line0 + l, hi, lo, e));
       }
       // ---- middle
       i64 ohi, olo;
@@ -114,7 +120,7 @@ struct Checker {
         for (i64 e = 0; e < N; ++e) {
           const i64 hb = ob + ohi * out.s_hi;
           if (out.map == IO_AFFINE || out.map == IO_GT) {
-            wr(out.buf, addr(out, ob, ohi, olo, e));
+            wr(out.buf, addr(out, ob, it.line0 + l, ohi, olo, e));
           } else if (out.map == IO_CHIRP) {
             const i64 q = olo * out.q_lo + e * out.q_e;
             if (q < out.mN) wr(out.buf, hb + q * out.s_t);
@@ -131,7 +137,7 @@ struct Checker {
           }
         }
       } else {
-        for (i64 e = 0; e < N; ++e) wr(out.buf, addr(out, ob, ohi, olo, e));
+        for (i64 e = 0; e < N; ++e) wr(out.buf, addr(out, ob, it.line0 + l, ohi, olo, e));
       }
     }
     if (d.kind == TILE_RADER && d.dlog) {

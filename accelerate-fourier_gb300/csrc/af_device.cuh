@@ -147,6 +147,7 @@ struct IoDesc {
   const float2* vec;
   i64 x0_off, x0_shi;  // IO_RADER: x0 at x0_off + hi*x0_shi in buffer x0_buf
   i64 dc_off;          // IO_RADER: DC of transform hi at ws[dc_off + hi]
+  const i64* loff;     // AFFINE views: when set, line l starts at loff[l] (gathered lines)
 };
 
 enum TileKind {

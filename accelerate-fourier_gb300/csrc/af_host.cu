@@ -127,6 +127,13 @@ TwTable PlanRes::table(i64 n) {
   return t;
 }
 
+const i64* PlanRes::line_table(const std::vector<i64>& offs) {
+  i64* p = (i64*)dalloc(sizeof(i64) * std::max<size_t>(offs.size(), 1));
+  if (dry) host_loffs[p] = offs;
+  else cuda_check(cudaMemcpy(p, offs.data(), sizeof(i64) * offs.size(), cudaMemcpyHostToDevice), "line table");
+  return p;
+}
+
 const float2* PlanRes::pair_table(i64 a, i64 b, int* off_b) {
   auto key = std::make_pair(a, b);
   TwTable ta = table(a), tb = table(b);
@@ -380,10 +387,10 @@ static IoDesc io_of(const View& v) {
 // entries) and per-line scratch (kMaxG lines), so that any mix of tiles in
 // one launch fits the shared memory the largest of them asked for.
 static const int kMaxTw = 512;
-static const int kMaxG = 256;
+static const int kMaxG = 128;
 static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, int* threads, int* G) {
   if (tw_total > kMaxTw) throw AfError(AF_ERR_UNSUPPORTED, "twiddle tables exceed the tile allowance");
-  const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - 8 * kMaxTw - 16 * kMaxG - 256;
+  const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - 8 * kMaxTw - 32 * kMaxG - 256;
   auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) <= budget; };
   // about 4096 elements per CTA keeps three CTAs resident per SM; strided
   // (line-fast) tiles take at least 4 lines, one 32-byte sector per row
@@ -1286,7 +1293,6 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   // single-tile launches are split by CTA size and shared-memory class, so
   // that small transforms are not held to the occupancy of large ones
   std::map<std::pair<int, int>, Launch> single;  // (threads * 2 + simple, smem class)
-  std::map<std::pair<i64, int>, int> single_desc;  // (n, threads) -> desc index
   auto single_key = [](const TileStep& s) {
     int c = 0;
     while ((1 << c) < spad_host(s.d.G * s.d.LS) + 2) ++c;
@@ -1297,28 +1303,14 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
     MultiPass mp;
   };
   std::vector<Big> bigs;
+  std::map<i64, std::vector<i64>> singles_by_n;  // single-tile transforms by length
   for (i64 i = 0; i < B->count; ++i) {
     const i64 n = B->ns[i];
     if (n == 0) continue;
     const Node* nd = B->planner.automatic(n);
     View in = View::rows(BUF_IN, 0, n, 1), out = View::rows(BUF_OUT, 0, n, 1);
     if (single_tile_ok(nd)) {
-      TileStep s = single_step(B->res, nd, sign, 1, in, out);
-      if (nd->n == 1) s = plain_step(B->res, 1, sign, 1, in, out);
-      s.d.cot = cot;
-      Launch& L = single[single_key(s)];
-      L.type = L_TILE;
-      auto key = std::make_pair(n, s.threads);
-      int di;
-      auto it = single_desc.find(key);
-      if (it == single_desc.end()) {
-        di = (int)L.descs.size();
-        L.descs.push_back(s.d);
-        single_desc[key] = di;
-      } else {
-        di = it->second;
-      }
-      append_tile(L, s, di, B->offs[i], B->offs[i]);
+      singles_by_n[n].push_back(i);
       continue;
     }
     Big b;
@@ -1354,6 +1346,28 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
       build_program(B->res, nd, sign, 1, &p);
       fallback.emplace_back(i, std::move(p));
     }
+  }
+  // Single-tile transforms of one length are the lines of one step: a
+  // gathered-line view (each line's offset from a table) lets a CTA take
+  // several small transforms at once.
+  for (auto& kv : singles_by_n) {
+    const i64 n = kv.first;
+    const std::vector<i64>& idx = kv.second;
+    const Node* nd = B->planner.automatic(n);
+    const i64 cnt = (i64)idx.size();
+    std::vector<i64> offs(idx.size());
+    for (size_t j = 0; j < idx.size(); ++j) offs[j] = B->offs[idx[j]];
+    const i64* lt = B->res.line_table(offs);
+    View in = View::rows(BUF_IN, 0, n, cnt), out = View::rows(BUF_OUT, 0, n, cnt);
+    TileStep s = n == 1 ? plain_step(B->res, 1, sign, cnt, in, out) : single_step(B->res, nd, sign, cnt, in, out);
+    s.d.in.loff = lt;
+    s.d.out.loff = lt;
+    s.d.cot = cot;
+    Launch& L = single[single_key(s)];
+    L.type = L_TILE;
+    const int di = (int)L.descs.size();
+    L.descs.push_back(s.d);
+    append_tile(L, s, di, 0, 0);
   }
   // Streams: (lane, CTA size class).  Lanes kLanes are the chunk pipelines,
   // lane kLanes holds the single-tile launches; classes are the CTA sizes

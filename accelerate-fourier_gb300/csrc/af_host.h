@@ -99,6 +99,7 @@ struct PlanRes {
   cudaStream_t stream = 0;                // stream for table generation and uploads
   unsigned long long fake_next = 1ull << 40;
   std::map<const void*, std::vector<int>> host_tabs;  // host copies of index tables
+  std::map<const void*, std::vector<i64>> host_loffs; // host copies of gathered-line tables
   std::vector<void*> allocs;
   std::map<i64, TwTable> tables;
   std::map<std::pair<i64, i64>, const float2*> pair_tables;
@@ -111,6 +112,7 @@ struct PlanRes {
   const float2* pair_table(i64 a, i64 b, int* off_b);
   const RaderRes& rader_res(i64 p, int sign);
   const ChirpRes& chirp_res(i64 len, i64 pad, int sign);
+  const i64* line_table(const std::vector<i64>& offs);  // device copy of line offsets
   void release();
 };
 

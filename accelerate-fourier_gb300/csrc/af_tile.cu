@@ -154,6 +154,19 @@ __device__ __forceinline__ i64 io_addr(const IoDesc& io, i64 base, int hi, int l
   if (io.map == IO_GT) return base + (i64)hi * io.s_hi + (i64)gt_index(io, lo, e) * io.s_t;
   return base + (i64)hi * io.s_hi + (i64)lo * io.s_lo + (i64)e * io.s_e;
 }
+// the same with the line's base offset lb already known (AFFINE views)
+__device__ __forceinline__ i64 io_addr_l(const IoDesc& io, i64 base, i64 lb, int hi, int lo, int e) {
+  if (io.map == IO_GT) return io_addr(io, base, hi, lo, e);
+  return base + lb + (i64)e * io.s_e;
+}
+// offset of line `line` of an AFFINE view (relative to the view's offset):
+// from the gathered-line table when the view has one
+__device__ __forceinline__ i64 line_base(const IoDesc& io, int line) {
+  if (io.loff) return __ldg(io.loff + line);
+  int hi, lo;
+  split_line(io, line, hi, lo);
+  return (i64)hi * io.s_hi + (i64)lo * io.s_lo;
+}
 
 // Visit (line, element) pairs of G lines x N elements in the coalescing
 // order asked for (element-fast or line-fast).
@@ -336,22 +349,17 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   const i64 ibase = in.off + it.in_add;
   const i64 obase = out.off + it.out_add;
 
-  // Per-line base offsets of AFFINE views (hi*s_hi + lo*s_lo, relative to
-  // the view's offset) for the CTA's G lines, input then output; PLAIN and
-  // CONVROW tiles keep them in the per-line scratch (16 bytes per line).
+  // Per-line base offsets of AFFINE views (relative to the view's offset)
+  // for the CTA's G lines, input then output, after the 2G slots of Rader
+  // scratch.
   const bool rows_kind = !GEN || d.kind == TILE_PLAIN || d.kind == TILE_CONVROW;
-  i64* lbi = reinterpret_cast<i64*>(xs);
-  i64* lbo = lbi + G;
-  if (rows_kind) {
-    for (int l = threadIdx.x; l < G; l += T) {
-      int hi, lo;
-      split_line(in, line0 + l, hi, lo);
-      lbi[l] = (i64)hi * in.s_hi + (i64)lo * in.s_lo;
-      split_line(out, line0 + l, hi, lo);
-      lbo[l] = (i64)hi * out.s_hi + (i64)lo * out.s_lo;
-    }
-    __syncthreads();
+  i64* lbi = reinterpret_cast<i64*>(xs + 2 * d.G);
+  i64* lbo = lbi + d.G;
+  for (int l = threadIdx.x; l < G; l += T) {
+    lbi[l] = line_base(in, line0 + l);
+    lbo[l] = line_base(out, line0 + l);
   }
+  __syncthreads();
   float lsum = 0.f;
 
   // ------------------------------------------------------------ load
@@ -451,7 +459,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
         const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
         pos = spad(l * d.LS + k * d.gt_n + j);
-        return c + io_addr(in, ibase, hi, lo, i);
+        return c + io_addr_l(in, ibase, lbi[l], hi, lo, i);
       }, sm);
     } else {
       load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
@@ -459,7 +467,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         split_line(in, line0 + l, hi, lo);
         const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
         const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
-        v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, i));
+        v = gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, i));
         return spad(l * d.LS + k * d.gt_n + j);
       }, sm);
     }
@@ -484,13 +492,13 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           const int lg = __ldg(&d.dlog[r - 1]);
           pos = spad(l * d.LS + (lg == 0 ? 0 : m - lg));
         }
-        return c + io_addr(in, ibase, hi, lo, r);
+        return c + io_addr_l(in, ibase, lbi[l], hi, lo, r);
       }, sm);
     } else {
       load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, float2& v) -> int {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
-        v = gldr(B, in.buf, io_addr(in, ibase, hi, lo, r));
+        v = gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, r));
         if (r == 0) return xs_pos + 2 * l;
         const int lg = __ldg(&d.dlog[r - 1]);
         return spad(l * d.LS + (lg == 0 ? 0 : m - lg));
@@ -502,7 +510,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
       v = make_float2(0.f, 0.f);
-      if (e < N) v = cmul(__ldg(&d.vec_a[e]), gldr(B, in.buf, io_addr(in, ibase, hi, lo, e)));
+      if (e < N) v = cmul(__ldg(&d.vec_a[e]), gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, e)));
       return spad(l * d.LS + e);
     }, sm);
   }
@@ -616,7 +624,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(out, line0 + l, hi, lo);
       const float2 v = sm[spad(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
                                (int)mod_of((unsigned)r, d.gt_n_mod))];
-      store_final(sc, out.buf, io_addr(out, obase, hi, lo, r), cscale(v, d.scale));
+      store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(v, d.scale));
     });
   } else if (d.kind == TILE_RADER) {
     // out[0] = x0 + sum res; out[r] = x0 + c[dlog r]  (Planned.hs:686-692)
@@ -625,14 +633,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(out, line0 + l, hi, lo);
       const float2 x0 = xs[2 * l];
       const float2 v = r == 0 ? xs[2 * l + 1] : sm[spad(l * d.LS + __ldg(&d.dlog[r - 1]))];
-      store_final(sc, out.buf, io_addr(out, obase, hi, lo, r), cscale(cadd(x0, v), d.scale));
+      store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(cadd(x0, v), d.scale));
     });
   } else {  // Bluestein: y = chirp * (take N c)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int e) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
       const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spad(l * d.LS + e)]);
-      store_final(sc, out.buf, io_addr(out, obase, hi, lo, e), cscale(v, d.scale));
+      store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, e), cscale(v, d.scale));
     });
   }
 
@@ -659,7 +667,7 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
   extern __shared__ float4 smem4[];
   float2* smem = reinterpret_cast<float2*>(smem4);
   const WorkItem it = items[blockIdx.x];
-  // shared layout: [descriptor] [A: smem_data] [B: smem_data] [tables] [scratch 2G]
+  // shared layout: [descriptor] [A: smem_data] [B: smem_data] [tables] [scratch 4G]
   TileDesc* d = reinterpret_cast<TileDesc*>(smem);
   {
     const int words = (int)(sizeof(TileDesc) / 4);
@@ -679,10 +687,10 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
   tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
-// descriptor, two buffers, tables, per-line scratch (at least 8 float2: the
-// loss reduction keeps one float per warp there)
+// descriptor, two buffers, tables, per-line scratch (4 float2 per line; at
+// least 8: the loss reduction keeps one float per warp there)
 size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
-  const int scratch = 2 * G > 8 ? 2 * G : 8;
+  const int scratch = 4 * G > 8 ? 4 * G : 8;  // Rader x0/sum pairs, then the line bases
   return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + scratch) * sizeof(float2);
 }
 
