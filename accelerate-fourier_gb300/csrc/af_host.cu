@@ -1282,7 +1282,7 @@ struct BatchPlan {
 };
 
 static const i64 kChunkElems = (i64)3 << 20;  // 24 MB of workspace per L2 chunk
-static const int kLanes = 2;                   // chunks in flight (48 MB of workspace in L2)
+static const int kLanes = 3;                   // chunks in flight (72 MB of workspace in L2)
 
 static void build_batch_program(BatchPlan* B, float sign, Program& prog,
                                 std::vector<std::pair<i64, Program>>& fallback, bool cot) {
@@ -1413,9 +1413,16 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   }
   lane_ws = (lane_ws + 63) / 64 * 64;
   std::vector<std::vector<int>> lane_last(kLanes);  // launches of the lane's previous chunk's last pass
+  // chunks go to the least-loaded lane (element-phases as the cost), largest
+  // chunks first, so that the lanes finish together
+  std::vector<double> lane_load(kLanes, 0.0);
   for (size_t c = 0; c < chunks.size(); ++c) {
     const size_t k = chunks[c].first, e = chunks[c].second;
-    const int lane = (int)(c % kLanes);
+    int lane = 0;
+    for (int l = 1; l < kLanes; ++l)
+      if (lane_load[l] < lane_load[lane]) lane = l;
+    for (size_t j = k; j < e; ++j)
+      for (const TileStep& st : bigs[j].mp.steps) lane_load[lane] += (double)st.lines * st.d.slen * std::max(1, st.d.nph);
     const i64 ws0 = lane * lane_ws;
     size_t maxsteps = 0;
     for (size_t j = k; j < e; ++j) maxsteps = std::max(maxsteps, bigs[j].mp.steps.size());
