@@ -65,3 +65,51 @@ def test_invalid_arguments_are_reported():
     with pytest.raises(_lib.AfError):
         _lib.plan_tree(12, "prep_dit2")  # not a power of two
     assert L.af_exec_c2c(None, 0, None, None, None, None, 1, None) == _lib.AF_ERR_INVALID
+
+
+def test_invalid_arguments_of_the_other_entry_points():
+    """Argument checks that fail before any device work (no GPU needed)."""
+    from accelerate_fourier import _lib
+    L = _lib.load()
+    INV = _lib.AF_ERR_INVALID
+    # null plans
+    assert L.af_exec_c2c_axis(None, 0, None, None, None, None, 1, 1, None) == INV
+    assert L.af_exec_c2c_2d(None, None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_exec_c2c_3d(None, None, None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_to_spectrum(None, None, 0, 0, None, None, 1, None) == INV
+    assert L.af_from_spectrum(None, 0, None, None, None, 1, None) == INV
+    assert L.af_vjp_to_spectrum(None, 0, None, None, None, 1, None) == INV
+    assert L.af_two_to_spectrum(None, None, None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_two_from_spectrum(None, 0, None, None, None, None, None, None, 1, None) == INV
+    assert L.af_convolve_cyclic(None, 0, None, None, None, None, None, None, 1, None) == INV
+    # negative sizes
+    assert L.af_karatsuba_i64(None, None, None, -1, 1, None) == INV
+    assert L.af_karatsuba_f32(None, None, None, 4, -1, None) == INV
+    assert L.af_conv_cyclic_fold_i64(None, None, -2, 1, None) == INV
+    assert L.af_untangle_spectra(0, None, None, None, None, None, None, -1, 1, None) == INV
+    assert L.af_untangle_spectra_2d(0, None, None, None, None, None, None, 2, -1, 1, None) == INV
+    assert L.af_entangle_spectra(0, None, None, None, None, None, None, 4, -1, None) == INV
+    assert L.af_cyclic_reverse_2d(0, None, None, None, None, -1, 2, 1, None) == INV
+    # null data with work to do
+    assert L.af_karatsuba_i32_i64(None, None, None, 8, 1, None) == INV
+    assert b"null" in L.af_last_error()
+    assert L.af_conv_complex_f64(0, None, None, None, None, None, None, 8, 1, None) == INV
+    # empty work is a no-op
+    assert L.af_karatsuba_i64(None, None, None, 0, 5, None) == _lib.AF_OK
+    assert L.af_untangle_spectra(0, None, None, None, None, None, None, 0, 3, None) == _lib.AF_OK
+
+
+def test_python_mirror_rejects_host_arrays():
+    """No CPU fallback: the transforms refuse arrays that are not on a GPU."""
+    torch = pytest.importorskip("torch")
+    from accelerate_fourier import _tensor, convolution, real
+    x = torch.zeros(8, dtype=torch.complex64)
+    with pytest.raises(ValueError):
+        _tensor.as_c64(x)
+    with pytest.raises(ValueError):
+        convolution.karatsuba(torch.zeros(1, 4, dtype=torch.int64), torch.zeros(1, 4, dtype=torch.int64))
+
+    class _Sub:
+        length = 4
+    with pytest.raises(ValueError):
+        real.toSpectrum(_Sub(), torch.zeros(1, 8))
