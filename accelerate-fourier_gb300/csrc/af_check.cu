@@ -83,7 +83,8 @@ struct Checker {
   void tile(const Launch& L, const TileDesc& d, const WorkItem& it) {
     const i64 G = it.G, N = d.nlen;
     if (G < 1 || G > d.G || it.line0 + G > d.nlines) fail("work item lines out of range");
-    if (spad_host(d.G * d.LS) + 2 > L.smem_data) fail("shared buffer too small");
+    if (spad_host(d.G * d.LS, d.pad_sh) + 2 > L.smem_data) fail("shared buffer too small");
+    if (d.pad_sh != 4 && d.pad_sh != 5 && d.pad_sh != 31) fail("bad padding shift");
     if (d.slen > d.LS) fail("shared line shorter than the transform");
     for (int p = 0; p < d.nph; ++p) check_phase(d, d.ph[p]);
     const IoDesc& in = d.in;
@@ -339,8 +340,8 @@ int afx_describe_batch(const int64_t* ns, int64_t count, int sign, int which, ch
         const TileDesc& d = L.descs[it.desc];
         elems += (i64)it.G * d.slen;
         char key[96];
-        snprintf(key, sizeof key, "k%d n%d s%d in%d out%d ph%d%s%s", d.kind, d.nlen, d.slen, d.in.map, d.out.map,
-                 d.nph, d.ptw ? " tw" : "", d.in.line_fast || d.out.line_fast ? " lf" : "");
+        snprintf(key, sizeof key, "k%d n%d s%d in%d out%d ph%d p%d%s%s", d.kind, d.nlen, d.slen, d.in.map, d.out.map,
+                 d.nph, d.pad_sh, d.ptw ? " tw" : "", d.in.line_fast || d.out.line_fast ? " lf" : "");
         kinds[key] += 1;
       }
       snprintf(line, sizeof line, "%zu tile T=%d ctas=%zu smem=%d elems=%lld descs=%zu :", k, L.threads,

@@ -196,6 +196,7 @@ struct TileDesc {
   // x0 capture (first pass of a multi-pass Rader): x[hi][0] of the step's
   // input goes to ws[x0_cap + out_add + hi] (x0_cap < 0: none)
   i64 x0_cap;
+  int pad_sh;        // shared-memory padding: one slot every 2^pad_sh elements
 };
 
 // One CTA's work in a launch: lines [line0, line0 + G) of descriptor `desc`;
@@ -209,8 +210,9 @@ struct WorkItem {
 };
 
 // ---------------------------------------------------------------- smem layout
-// One padding slot every 16 float2 keeps strided Stockham writes bank friendly.
-__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+// One padding slot every 2^sh float2 keeps strided Stockham accesses off bank
+// conflicts; each tile picks sh (sh = 31: no padding).
+__device__ __forceinline__ int spd_(int i, int sh) { return i + (i >> sh); }
 
 // ---------------------------------------------------------------- twiddles
 // Tables hold the forward root: tab[t] = exp(-2*pi*i*t/n), as two levels

@@ -413,6 +413,65 @@ struct TileStep {
   i64 lines = 0;
 };
 
+// Shared-memory wavefronts of a tile's Stockham passes for padding shift sh,
+// from a sample of warps of every pass (64-bit accesses served per half-warp:
+// one wavefront per distinct address on the busiest of the 16 float2 banks).
+static i64 pad_cost(const TileDesc& d, int G, int sh) {
+  i64 cost = 0;
+  int a[32];
+  for (int ph = 0; ph < d.nph; ++ph) {
+    const FftPhase& f = d.ph[ph];
+    const int lines = G * f.lcnt;
+    for (int ps = 0; ps < f.npass; ++ps) {
+      const int R = f.pass[ps].R, p = f.pass[ps].p, nb = f.n / R;
+      const int total = lines * nb;
+      const int warps = (total + 31) / 32;
+      const int step = std::max(1, warps / 8);
+      for (int w = 0; w < warps; w += step) {
+        for (int rw = 0; rw < 2; ++rw)
+          for (int j = 0; j < R; ++j) {
+            int cnt = 0;
+            for (int g = 32 * w; g < std::min(total, 32 * w + 32); ++g) {
+              const int l = g / nb, i = g - l * nb;
+              const int t = l / f.lcnt;
+              const int base = t * d.LS + (l - t * f.lcnt) * f.ls;
+              const int q = i / p, k = i - q * p;
+              const int e = rw == 0 ? base + (i + j * nb) * f.es : base + (q * p * R + k + j * p) * f.es;
+              a[cnt++] = spad_host(e, sh);
+            }
+            for (int h = 0; h < cnt; h += 16) {
+              int worst = 0;
+              for (int b = 0; b < 16; ++b) {
+                int distinct = 0;
+                for (int x = h; x < std::min(cnt, h + 16); ++x) {
+                  if ((a[x] & 15) != b) continue;
+                  bool seen = false;
+                  for (int y = h; y < x; ++y) seen = seen || a[y] == a[x];
+                  distinct += !seen;
+                }
+                worst = std::max(worst, distinct);
+              }
+              cost += worst;
+            }
+          }
+      }
+    }
+  }
+  return cost;
+}
+
+// The padding with the fewest sampled shared-memory wavefronts; never more
+// padding than one slot per 16 (the geometry was sized for that).
+static int choose_pad(const TileDesc& d) {
+  int best = 4;
+  i64 bc = pad_cost(d, d.G, 4);
+  for (int sh : {5, 31}) {
+    const i64 c = pad_cost(d, d.G, sh);
+    if (c < bc) { bc = c; best = sh; }
+  }
+  return best;
+}
+
 static void finish_geometry(TileStep& s, i64 slen, bool want_wide) {
   int threads, G;
   choose_geometry(slen, s.lines, s.d.tw_total, want_wide, &threads, &G);
@@ -422,11 +481,13 @@ static void finish_geometry(TileStep& s, i64 slen, bool want_wide) {
   s.d.G_div = make_fastdiv((unsigned)G);
   s.d.N_div = make_fastdiv((unsigned)s.d.nlen);
   s.d.S_div = make_fastdiv((unsigned)s.d.slen);
+  s.d.pad_sh = choose_pad(s.d);
 }
 
 static TileDesc blank_desc() {
   TileDesc d;
   memset(&d, 0, sizeof d);
+  d.pad_sh = 4;
   d.scale = 1.f;
   d.dc_off = -1;
   d.x0_cap = -1;
@@ -863,7 +924,7 @@ static Launch launch_of(const TileStep& s) {
     w.G = (int)std::min<i64>(s.d.G, s.lines - l0);
     L.items.push_back(w);
   }
-  L.smem_data = spad_host(s.d.G * s.d.LS) + 2;
+  L.smem_data = spad_host(s.d.G * s.d.LS, s.d.pad_sh) + 2;
   L.tw_max = s.d.tw_total;
   L.g_max = s.d.G;
   return L;
@@ -880,7 +941,7 @@ static void append_tile(Launch& L, const TileStep& s, int desc_index, i64 in_add
     w.out_add = out_add;
     L.items.push_back(w);
   }
-  L.smem_data = std::max(L.smem_data, spad_host(s.d.G * s.d.LS) + 2);
+  L.smem_data = std::max(L.smem_data, spad_host(s.d.G * s.d.LS, s.d.pad_sh) + 2);
   L.tw_max = std::max(L.tw_max, s.d.tw_total);
   L.g_max = std::max(L.g_max, s.d.G);
   L.threads = std::max(L.threads, s.threads);
@@ -1295,7 +1356,7 @@ static void build_batch_program(BatchPlan* B, float sign, Program& prog,
   std::map<std::pair<int, int>, Launch> single;  // (threads * 2 + simple, smem class)
   auto single_key = [](const TileStep& s) {
     int c = 0;
-    while ((1 << c) < spad_host(s.d.G * s.d.LS) + 2) ++c;
+    while ((1 << c) < spad_host(s.d.G * s.d.LS, s.d.pad_sh) + 2) ++c;
     return std::make_pair(s.threads * 2 + (simple_desc(s.d) ? 1 : 0), c);
   };
   struct Big {

@@ -6,7 +6,7 @@
 
 namespace af {
 
-__host__ __device__ __forceinline__ int spad_host(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int spad_host(int i, int sh = 4) { return i + (i >> sh); }
 
 // ------------------------------------------------------------- tile kernel
 // One launch of the tile kernel: `nitems` CTAs, item i runs descs[items[i].desc].

@@ -25,7 +25,7 @@ namespace af {
 // Scalars of one phase, held in registers (the descriptor lives in shared
 // memory; reading its fields inside the pass loops would re-read them).
 struct PhaseRegs {
-  int n, lines, LS, ls, es, lcnt, S_log2;
+  int n, lines, LS, ls, es, lcnt, S_log2, psh;
   float sign;
   FastDiv lcnt_div;
 };
@@ -75,14 +75,14 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
     float2 u[R];
     const int ib = base + i * ph.es;
 #pragma unroll
-    for (int j = 0; j < R; ++j) u[j] = src[spad(ib + j * nbe)];
+    for (int j = 0; j < R; ++j) u[j] = src[spd_(ib + j * nbe, ph.psh)];
     const int q = (int)fdiv((unsigned)i, pdv);
     const int k = i - q * p;
     if (k > 0) apply_twiddles<R>(u, ptab, ph.S_log2, k * tws, ph.sign);
     Dft<R>::run(u, ph.sign, ptab, ph.S_log2, ph.n);
     const int ob = base + (q * p * R + k) * ph.es;
 #pragma unroll
-    for (int j = 0; j < R; ++j) dst[spad(ob + j * pe)] = u[j];
+    for (int j = 0; j < R; ++j) dst[spd_(ob + j * pe, ph.psh)] = u[j];
   }
   __syncthreads();
 }
@@ -90,8 +90,9 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
 // Runs every pass of a phase; returns the buffer holding the result.
 template <int T>
 __device__ __forceinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
-                                             const float2* tab) {
+                                             const float2* tab, int psh) {
   PhaseRegs r;
+  r.psh = psh;
   r.n = phs->n;
   r.lines = G * phs->lcnt;
   r.LS = LS;
@@ -241,7 +242,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 template <int T, class F>
 __device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndiv, const FastDiv& Gdiv,
-                                                int line_fast, int LS, F src, float2* sm) {
+                                                int line_fast, int LS, int psh, F src, float2* sm) {
   const int tot = G * N;
   for (int q = threadIdx.x; q < tot; q += T) {
     int l, e;
@@ -252,7 +253,7 @@ __device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndi
       e = (int)fdiv((unsigned)q, Gdiv);
       l = q - e * G;
     }
-    int pos = spad(l * LS + e);  // src may move the element (permuted tiles)
+    int pos = spd_(l * LS + e, psh);  // src may move the element (permuted tiles)
     const float2* g = src(l, e, pos);
     float2* d = sm + pos;
     if (g) cp_async8(d, g);
@@ -335,6 +336,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   const int line0 = it.line0;
   const int G = it.G;
   const int N = d.nlen;
+  const int psh = d.pad_sh;
   FastDiv Gdiv = d.G_div;
   if (G != d.G) {
     Gdiv.d = G;
@@ -375,27 +377,27 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           const float2* c = r.c;
           const i64 se = r.s_e;
           if (se == 1)
-            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) { return c + lbi[l] + e; }, sm);
+            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) { return c + lbi[l] + e; }, sm);
           else
-            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS,
+            load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh,
                                [&](int l, int e, int&) { return c + lbi[l] + (i64)e * se; }, sm);
         } else if (r.s_e == 1) {
           load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
             v = rld(r, lbi[l] + e);
-            return spad(l * LS + e);
+            return spd_(l * LS + e, psh);
           }, sm);
         } else {
           const i64 se = r.s_e;
           load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
             v = rld(r, lbi[l] + (i64)e * se);
-            return spad(l * LS + e);
+            return spd_(l * LS + e, psh);
           }, sm);
         }
         break;
       case IO_GT:
         if (r.c) {
           const float2* c = r.c;
-          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) {
+          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) {
             int hi, lo;
             rsplit(r, line0 + l, hi, lo);
             return c + (i64)hi * r.s_hi + (i64)rgt(r, lo, e) * r.s_t;
@@ -406,14 +408,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
           v = rld(r, (i64)hi * r.s_hi + (i64)rgt(r, lo, e) * r.s_t);
-          return spad(l * LS + e);
+          return spd_(l * LS + e, psh);
         }, sm);
         break;
       case IO_TABLE:  // zero beyond the table length mN
         if (r.c) {
           const float2* c = r.c;
           const float2* zero = nullptr;
-          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, [&](int l, int e, int&) {
+          load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) {
             int hi, lo;
             rsplit(r, line0 + l, hi, lo);
             const i64 q = lo * r.q_lo + e * r.q_e;
@@ -427,7 +429,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           const i64 q = lo * r.q_lo + e * r.q_e;
           v = make_float2(0.f, 0.f);
           if (q < r.mN) v = rld(r, (i64)hi * r.s_hi + (i64)__ldg(&r.tab[q]) * r.s_t);
-          return spad(l * LS + e);
+          return spd_(l * LS + e, psh);
         }, sm);
         break;
       default:  // IO_CHIRP: zero pad beyond the logical length
@@ -437,7 +439,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           const i64 q = lo * r.q_lo + e * r.q_e;
           v = make_float2(0.f, 0.f);
           if (q < r.mN) v = cmul(__ldg(&r.vec[q]), rld(r, (i64)hi * r.s_hi + q * r.s_t));
-          return spad(l * LS + e);
+          return spd_(l * LS + e, psh);
         }, sm);
         break;
     }
@@ -453,12 +455,12 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     // inverting: k = i*cm mod m, j = i*cn mod n
     if (B.c[in.buf]) {
       const float2* c = B.c[in.buf];
-      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, [&](int l, int i, int& pos) {
+      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, psh, [&](int l, int i, int& pos) {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
         const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
         const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
-        pos = spad(l * d.LS + k * d.gt_n + j);
+        pos = spd_(l * d.LS + k * d.gt_n + j, psh);
         return c + io_addr_l(in, ibase, lbi[l], hi, lo, i);
       }, sm);
     } else {
@@ -468,7 +470,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
         const int j = (int)mulmod((unsigned)i, (unsigned)d.gt_cn, d.gt_n_mod);
         v = gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, i));
-        return spad(l * d.LS + k * d.gt_n + j);
+        return spd_(l * d.LS + k * d.gt_n + j, psh);
       }, sm);
     }
   } else if (d.kind == TILE_RADER) {
@@ -478,19 +480,19 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     // a convolution carried by longer transforms (slen > p-1) is zero padded
     for (int q = threadIdx.x; q < G * (d.slen - m); q += T) {
       const int l = q / (d.slen - m);
-      sm[spad(l * d.LS + m + (q - l * (d.slen - m)))] = make_float2(0.f, 0.f);
+      sm[spd_(l * d.LS + m + (q - l * (d.slen - m)), psh)] = make_float2(0.f, 0.f);
     }
     const int xs_pos = (int)(xs - sm);  // x0 of line l goes to xs[2 l]
     if (B.c[in.buf]) {
       const float2* c = B.c[in.buf];
-      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, [&](int l, int r, int& pos) {
+      load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, psh, [&](int l, int r, int& pos) {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
         if (r == 0) {
           pos = xs_pos + 2 * l;
         } else {
           const int lg = __ldg(&d.dlog[r - 1]);
-          pos = spad(l * d.LS + (lg == 0 ? 0 : m - lg));
+          pos = spd_(l * d.LS + (lg == 0 ? 0 : m - lg), psh);
         }
         return c + io_addr_l(in, ibase, lbi[l], hi, lo, r);
       }, sm);
@@ -501,7 +503,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         v = gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, r));
         if (r == 0) return xs_pos + 2 * l;
         const int lg = __ldg(&d.dlog[r - 1]);
-        return spad(l * d.LS + (lg == 0 ? 0 : m - lg));
+        return spd_(l * d.LS + (lg == 0 ? 0 : m - lg), psh);
       }, sm);
     }
   } else {  // TILE_BLUESTEIN: chirp * x zero padded to M (Planned.hs:765-773)
@@ -511,7 +513,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       split_line(in, line0 + l, hi, lo);
       v = make_float2(0.f, 0.f);
       if (e < N) v = cmul(__ldg(&d.vec_a[e]), gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, e)));
-      return spad(l * d.LS + e);
+      return spd_(l * d.LS + e, psh);
     }, sm);
   }
   cp_async_wait_all();  // tables (and any tile copies not yet waited for)
@@ -525,7 +527,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       // FFT(+1) -> * spectrum -> FFT(-1): the direction order of the reference's
       // convolveSingleSpectrumCyclicCache (Planned.hs:803-821)
       if (d.kind == TILE_RADER) {
-        for (int l = threadIdx.x; l < G; l += T) xs[2 * l + 1] = sm[spad(l * d.LS)];  // sum res
+        for (int l = threadIdx.x; l < G; l += T) xs[2 * l + 1] = sm[spd_(l * d.LS, psh)];  // sum res
         __syncthreads();
       }
       const int M = d.slen;
@@ -534,25 +536,25 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           for (int l = 0; l < G; ++l) {
             int hi, lo;
             split_line(out, line0 + l, hi, lo);
-            if (lo == 0) B.c[BUF_WS][d.dc_off + it.out_add + hi] = sm[spad(l * d.LS)];
+            if (lo == 0) B.c[BUF_WS][d.dc_off + it.out_add + hi] = sm[spd_(l * d.LS, psh)];
           }
         }
         __syncthreads();
         for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
           int hi, lo;
           split_line(out, line0 + l, hi, lo);
-          const int a = spad(l * d.LS + e);
+          const int a = spd_(l * d.LS + e, psh);
           sm[a] = cmul(__ldg(&d.vec_b[lo * d.sq_lo + e * d.sq_e]), sm[a]);
         });
       } else {
         for_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e) {
-          const int a = spad(l * d.LS + e);
+          const int a = spd_(l * d.LS + e, psh);
           sm[a] = cmul(__ldg(&d.vec_b[e]), sm[a]);
         });
       }
       __syncthreads();
     }
-    sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[phi], d.LS, G, tab);
+    sm = run_phase<T>(sm, sm == A ? Bf : A, &d.ph[phi], d.LS, G, tab, psh);
   }
 
   // ------------------------------------------------------------ store
@@ -588,7 +590,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       } else {
         rsplit(ro, line0 + l, hi, lo);
       }
-      float2 v = sm[spad(l * LS + e)];
+      float2 v = sm[spd_(l * LS + e, psh)];
       if (ptw) {
         const unsigned t = mulmod((unsigned)lo, (unsigned)e, pmod);
         const float2 wl = __ldg(&ptw[t & ((1u << ptwS) - 1)]);
@@ -622,8 +624,8 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 v = sm[spad(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
-                               (int)mod_of((unsigned)r, d.gt_n_mod))];
+      const float2 v = sm[spd_(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
+                               (int)mod_of((unsigned)r, d.gt_n_mod), psh)];
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(v, d.scale));
     });
   } else if (d.kind == TILE_RADER) {
@@ -632,14 +634,14 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
       const float2 x0 = xs[2 * l];
-      const float2 v = r == 0 ? xs[2 * l + 1] : sm[spad(l * d.LS + __ldg(&d.dlog[r - 1]))];
+      const float2 v = r == 0 ? xs[2 * l + 1] : sm[spd_(l * d.LS + __ldg(&d.dlog[r - 1]), psh)];
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(cadd(x0, v), d.scale));
     });
   } else {  // Bluestein: y = chirp * (take N c)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int e) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spad(l * d.LS + e)]);
+      const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spd_(l * d.LS + e, psh)]);
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, e), cscale(v, d.scale));
     });
   }
