@@ -84,7 +84,7 @@ struct Checker {
     const i64 G = it.G, N = d.nlen;
     if (G < 1 || G > d.G || it.line0 + G > d.nlines) fail("work item lines out of range");
     if (spad_host(d.G * d.LS, d.pad_sh) + 2 > L.smem_data) fail("shared buffer too small");
-    if (d.pad_sh != 4 && d.pad_sh != 5 && d.pad_sh != 31) fail("bad padding shift");
+    if (d.pad_sh < 4 || d.pad_sh > 31) fail("bad padding shift");
     if (d.slen > d.LS) fail("shared line shorter than the transform");
     for (int p = 0; p < d.nph; ++p) check_phase(d, d.ph[p]);
     const IoDesc& in = d.in;

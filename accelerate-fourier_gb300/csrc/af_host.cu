@@ -8,6 +8,8 @@
 #include <complex>
 #include <cstring>
 #include <functional>
+#include <map>
+#include <mutex>
 
 namespace af {
 
@@ -413,62 +415,84 @@ struct TileStep {
   i64 lines = 0;
 };
 
-// Shared-memory wavefronts of a tile's Stockham passes for padding shift sh,
-// from a sample of warps of every pass (64-bit accesses served per half-warp:
-// one wavefront per distinct address on the busiest of the 16 float2 banks).
-static i64 pad_cost(const TileDesc& d, int G, int sh) {
+// Wavefronts of one half-warp's 64-bit shared accesses: the busiest of the
+// 16 float2 banks serves one wavefront per distinct address.
+static int half_warp_wavefronts(int* a, int cnt) {
+  std::sort(a, a + cnt);
+  int per_bank[16] = {0}, worst = 0;
+  for (int x = 0; x < cnt; ++x)
+    if (x == 0 || a[x] != a[x - 1]) worst = std::max(worst, ++per_bank[a[x] & 15]);
+  return worst;
+}
+
+// Shared-memory wavefronts of a tile for padding shift sh, from a sample of
+// warps: the tile load and store (element- or line-fast) and every Stockham
+// pass's reads and writes.
+static i64 pad_cost(const TileDesc& d, int sh) {
+  const int G = d.G;
   i64 cost = 0;
-  int a[32];
+  int a[16];
+  auto warp = [&](auto&& addr, int first, int total) {
+    for (int h = first; h < std::min(total, first + 32); h += 16) {
+      int cnt = 0;
+      for (int g = h; g < std::min(total, h + 16); ++g) a[cnt++] = spad_host(addr(g), sh);
+      cost += half_warp_wavefronts(a, cnt);
+    }
+  };
+  auto sampled = [&](int total, auto&& body) {
+    const int warps = (total + 31) / 32, step = std::max(1, warps / 4);
+    for (int w = 0; w < warps; w += step) body(32 * w);
+  };
+  const int N = d.nlen, tot = G * N;
+  for (int lf : {d.in.line_fast, d.out.line_fast})
+    sampled(tot, [&](int first) {
+      warp([&](int q) { return lf ? (q % G) * d.LS + q / G : (q / N) * d.LS + q % N; }, first, tot);
+    });
   for (int ph = 0; ph < d.nph; ++ph) {
     const FftPhase& f = d.ph[ph];
-    const int lines = G * f.lcnt;
     for (int ps = 0; ps < f.npass; ++ps) {
       const int R = f.pass[ps].R, p = f.pass[ps].p, nb = f.n / R;
-      const int total = lines * nb;
-      const int warps = (total + 31) / 32;
-      const int step = std::max(1, warps / 8);
-      for (int w = 0; w < warps; w += step) {
-        for (int rw = 0; rw < 2; ++rw)
-          for (int j = 0; j < R; ++j) {
-            int cnt = 0;
-            for (int g = 32 * w; g < std::min(total, 32 * w + 32); ++g) {
-              const int l = g / nb, i = g - l * nb;
-              const int t = l / f.lcnt;
+      const int total = G * f.lcnt * nb;
+      sampled(total, [&](int first) {
+        for (int j = 0; j < R; ++j)
+          for (int rw = 0; rw < 2; ++rw)
+            warp([&](int g) {
+              const int l = g / nb, i = g - l * nb, t = l / f.lcnt;
               const int base = t * d.LS + (l - t * f.lcnt) * f.ls;
               const int q = i / p, k = i - q * p;
-              const int e = rw == 0 ? base + (i + j * nb) * f.es : base + (q * p * R + k + j * p) * f.es;
-              a[cnt++] = spad_host(e, sh);
-            }
-            for (int h = 0; h < cnt; h += 16) {
-              int worst = 0;
-              for (int b = 0; b < 16; ++b) {
-                int distinct = 0;
-                for (int x = h; x < std::min(cnt, h + 16); ++x) {
-                  if ((a[x] & 15) != b) continue;
-                  bool seen = false;
-                  for (int y = h; y < x; ++y) seen = seen || a[y] == a[x];
-                  distinct += !seen;
-                }
-                worst = std::max(worst, distinct);
-              }
-              cost += worst;
-            }
-          }
-      }
+              return base + (rw == 0 ? i + j * nb : q * p * R + k + j * p) * f.es;
+            }, first, total);
+      });
     }
   }
   return cost;
 }
 
-// The padding with the fewest sampled shared-memory wavefronts; never more
-// padding than one slot per 16 (the geometry was sized for that).
+// The padding shift (one slot per 2^sh elements; 31 = none) with the fewest
+// sampled shared-memory wavefronts.  Never more padding than one slot per 16:
+// the geometry was sized for that.  Tiles of the same shape share the answer.
 static int choose_pad(const TileDesc& d) {
+  std::vector<int> key = {d.G, d.LS, d.nlen, d.in.line_fast, d.out.line_fast, d.nph};
+  for (int ph = 0; ph < d.nph; ++ph) {
+    const FftPhase& f = d.ph[ph];
+    key.insert(key.end(), {f.n, f.lcnt, f.ls, f.es, f.npass});
+    for (int ps = 0; ps < f.npass; ++ps) key.insert(key.end(), {f.pass[ps].R, f.pass[ps].p});
+  }
+  static std::mutex mu;
+  static std::map<std::vector<int>, int> memo;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+  }
   int best = 4;
-  i64 bc = pad_cost(d, d.G, 4);
-  for (int sh : {5, 31}) {
-    const i64 c = pad_cost(d, d.G, sh);
+  i64 bc = pad_cost(d, 4);
+  for (int sh : {5, 6, 7, 8, 9, 10, 31}) {
+    const i64 c = pad_cost(d, sh);
     if (c < bc) { bc = c; best = sh; }
   }
+  std::lock_guard<std::mutex> g(mu);
+  memo[key] = best;
   return best;
 }
 
