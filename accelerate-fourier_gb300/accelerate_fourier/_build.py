@@ -43,6 +43,9 @@ def _headers_mtime() -> float:
 
 def _compile(src: str, nvcc: str, hdr_mtime: float) -> str:
     obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+    if src.endswith("64.cu"):
+        # the FP64 builds include another translation unit of csrc/
+        hdr_mtime = max(hdr_mtime, *(os.path.getmtime(s) for s in sources()))
     if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
             and os.path.getmtime(obj) >= hdr_mtime):
         return obj

@@ -38,6 +38,11 @@ SIGNATURES = {
     "af_plan_tree": ([I64, INT, ctypes.c_char_p, ctypes.c_size_t], INT),
     "af_plan_launches": ([PTR, I64, ctypes.POINTER(I64)], INT),
     "af_exec_c2c": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_plan_create_f64": ([ctypes.POINTER(PTR), I64, INT, INT], INT),
+    "af_exec_c2c_f64": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_vjp_c2c_f64": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_exec_c2c_2d_f64": ([PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_exec_c2c_3d_f64": ([PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_vjp_c2c": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_scale_down": ([INT, PTR, PTR, I64, I64, PTR], INT),
     "af_cyclic_reverse": ([INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
@@ -125,14 +130,17 @@ def plan_tree(n: int, algo: str = "auto") -> str:
 
 
 class Plan:
-    """An af_plan: a reference plan tree with its device tables."""
+    """An af_plan: a reference plan tree with its device tables, over
+    Complex Float, or Complex Double when `double` is set."""
 
-    def __init__(self, n: int, sign: int, algo: str = "auto"):
+    def __init__(self, n: int, sign: int, algo: str = "auto", double: bool = False):
         self._h = PTR()
         self.n = int(n)
         self.sign = int(sign)
         self.algo = algo
-        check(load().af_plan_create(ctypes.byref(self._h), self.n, self.sign, ALGO[algo]))
+        self.double = bool(double)
+        create = load().af_plan_create_f64 if self.double else load().af_plan_create
+        check(create(ctypes.byref(self._h), self.n, self.sign, ALGO[algo]))
 
     @property
     def handle(self):
@@ -149,7 +157,11 @@ class Plan:
         return out.value
 
     def exec_ptr(self, src_re, src_im, dst_re, dst_im, batch, stream=0, layout=INTERLEAVED, vjp=False):
-        f = load().af_vjp_c2c if vjp else load().af_exec_c2c
+        lib = load()
+        if self.double:
+            f = lib.af_vjp_c2c_f64 if vjp else lib.af_exec_c2c_f64
+        else:
+            f = lib.af_vjp_c2c if vjp else lib.af_exec_c2c
         check(f(self._h, layout, src_re, src_im, dst_re, dst_im, batch, stream))
 
     def __del__(self):

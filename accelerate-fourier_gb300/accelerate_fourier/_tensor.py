@@ -3,7 +3,8 @@
 Arrays follow the reference's convention: the transform runs over the last
 axis, every leading axis is batch.  Complex data is a complex64 tensor
 (interleaved) or a pair (re, im) of float32 tensors (planar, Accelerate's own
-layout of `Array sh (Complex Float)`).
+layout of `Array sh (Complex Float)`); the planned transforms also take
+Complex Double (complex128, or a pair of float64 tensors).
 """
 from __future__ import annotations
 
@@ -36,10 +37,18 @@ def rows(x: torch.Tensor):
     return int(n), int(batch)
 
 
-def run_plan(plan: "_lib.Plan", x, vjp: bool = False, out=None):
-    """Apply an af_plan to the last axis of x (complex64 tensor or (re, im))."""
+def is_double(x) -> bool:
+    """Complex Double data: a complex128 tensor or a pair of float64 tensors."""
     if isinstance(x, tuple):
-        re, im = (t.contiguous().to(torch.float32) for t in x)
+        return x[0].dtype == torch.float64
+    return x.dtype == torch.complex128
+
+
+def run_plan(plan: "_lib.Plan", x, vjp: bool = False, out=None):
+    """Apply an af_plan to the last axis of x (complex64 tensor or (re, im);
+    complex128 or float64 pairs for a Complex Double plan)."""
+    if isinstance(x, tuple):
+        re, im = (t.contiguous().to(torch.float64 if plan.double else torch.float32) for t in x)
         require_cuda(re)
         n, batch = rows(re)
         if n != plan.n:
@@ -50,7 +59,11 @@ def run_plan(plan: "_lib.Plan", x, vjp: bool = False, out=None):
             plan.exec_ptr(re.data_ptr(), im.data_ptr(), ore.data_ptr(), oim.data_ptr(), batch,
                           stream_ptr(), _lib.PLANAR, vjp)
         return ore, oim
-    x = as_c64(x)
+    if plan.double:
+        require_cuda(x)
+        x = x.to(torch.complex128).contiguous()
+    else:
+        x = as_c64(x)
     n, batch = rows(x)
     if n != plan.n:
         raise ValueError(f"length {n} does not match plan length {plan.n}")

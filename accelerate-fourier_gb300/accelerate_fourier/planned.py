@@ -15,7 +15,12 @@ from .sign import check, forward, inverse  # noqa: F401
 
 
 class Transform:
-    """`Transform sh a = Acc (Array sh a) -> Acc (Array sh a)` (Private.hs:29)."""
+    """`Transform sh a = Acc (Array sh a) -> Acc (Array sh a)` (Private.hs:29).
+
+    Like the reference's transforms (polymorphic over `A.RealFloat a`), one
+    Transform applies to Complex Float and Complex Double arrays: complex128
+    data (or float64 planes) runs on a Complex Double plan of the same tree,
+    made on first use."""
 
     def __init__(self, sign: int, length: int, algo: str = "auto"):
         self.sign = check(sign)
@@ -23,20 +28,25 @@ class Transform:
         self.algo = algo
         self.plan = _plan(self.sign, self.length, algo)
 
+    def plan_for(self, x) -> _lib.Plan:
+        if _tensor.is_double(x):
+            return _plan(self.sign, self.length, self.algo, True)
+        return self.plan
+
     def __call__(self, x, out=None):
-        return _tensor.run_plan(self.plan, x, out=out)
+        return _tensor.run_plan(self.plan_for(x), x, out=out)
 
     def vjp(self, cotangent, out=None):
         """Adjoint: DFT^H applied to the cotangent (unscaled opposite-sign transform)."""
-        return _tensor.run_plan(self.plan, cotangent, vjp=True, out=out)
+        return _tensor.run_plan(self.plan_for(cotangent), cotangent, vjp=True, out=out)
 
     def describe(self) -> str:
         return self.plan.describe()
 
 
 @functools.lru_cache(maxsize=256)
-def _plan(sign: int, length: int, algo: str) -> _lib.Plan:
-    return _lib.Plan(length, sign, algo)
+def _plan(sign: int, length: int, algo: str, double: bool = False) -> _lib.Plan:
+    return _lib.Plan(length, sign, algo, double)
 
 
 def transform(sign: int, length: int) -> Transform:
@@ -99,10 +109,11 @@ class TransformND:
         import torch
         lib = _lib.load()
         d = len(self.transforms)
+        double = _tensor.is_double(x)
         if isinstance(x, tuple):
-            re, im = (t.contiguous().to(torch.float32) for t in x)
+            re, im = (t.contiguous().to(torch.float64 if double else torch.float32) for t in x)
             _tensor.require_cuda(re)
-            *plans, batch = self.shape_check(re.shape)
+            *_, batch = self.shape_check(re.shape)
             ore = torch.empty_like(re) if out is None else out[0]
             oim = torch.empty_like(im) if out is None else out[1]
             args = (_lib.PLANAR, re.data_ptr(), im.data_ptr(), ore.data_ptr(), oim.data_ptr(), batch,
@@ -110,15 +121,19 @@ class TransformND:
             res = (ore, oim)
             n = re.numel()
         else:
-            x = _tensor.as_c64(x)
-            *plans, batch = self.shape_check(x.shape)
+            _tensor.require_cuda(x)
+            x = x.contiguous() if double else _tensor.as_c64(x)
+            *_, batch = self.shape_check(x.shape)
             y = torch.empty_like(x) if out is None else out
             args = (_lib.INTERLEAVED, x.data_ptr(), None, y.data_ptr(), None, batch, _tensor.stream_ptr())
             res = y
             n = x.numel()
         if n:
-            handles = [p.handle for p in plans]
-            f = lib.af_exec_c2c_2d if d == 2 else lib.af_exec_c2c_3d
+            handles = [t.plan_for(x).handle for t in self.transforms]
+            if double:
+                f = lib.af_exec_c2c_2d_f64 if d == 2 else lib.af_exec_c2c_3d_f64
+            else:
+                f = lib.af_exec_c2c_2d if d == 2 else lib.af_exec_c2c_3d
             _lib.check(f(*handles, *args))
         return res
 

@@ -34,6 +34,7 @@ void af::set_last_error(const std::string& m) { g_err = m; }
   catch (const std::exception& e) { return fail(AF_ERR_INVALID, e.what()); }
 
 af_plan_s::~af_plan_s() {
+  if (p64) af64::plan_destroy(p64);
   if (ws) cudaFree(ws);
   if (stage) cudaFree(stage);
   res.release();
@@ -75,7 +76,12 @@ const Node* plan_root(Planner& pl, i64 n, int algo) {
 }
 }  // namespace af
 
+static void need_f32(const af_plan_s* P) {
+  if (P->p64) throw AfError(AF_ERR_INVALID, "the plan is Complex Double: use the _f64 entry points");
+}
+
 static Program& program_for(af_plan_s* P, i64 batch, int sign) {
+  need_f32(P);
   auto key = std::make_pair((long long)batch, sign);
   auto it = P->progs.find(key);
   if (it != P->progs.end()) return it->second;
@@ -95,6 +101,7 @@ static void ensure_ws(af_plan_s* P, i64 elems) {
 // Program of the plan's tree along the middle axis of an (outer, n, inner)
 // array (inner = 1: contiguous rows).
 static Program& axis_program(af_plan_s* P, i64 outer, i64 inner, int sign) {
+  need_f32(P);
   if (inner == 1) return program_for(P, outer, sign);
   auto key = std::make_tuple((long long)outer, (long long)inner, sign);
   auto it = P->axis_progs.find(key);
@@ -218,6 +225,64 @@ af_status af_plan_create(af_plan* plan, int64_t n, int sign, af_algo algo) {
   AF_CATCH
 }
 
+af_status af_plan_create_f64(af_plan* plan, int64_t n, int sign, af_algo algo) {
+  AF_TRY
+  if (!plan) return fail(AF_ERR_INVALID, "null plan pointer");
+  *plan = nullptr;
+  if (n < 0) return fail(AF_ERR_INVALID, "negative size");
+  if (sign != 1 && sign != -1) return fail(AF_ERR_INVALID, "sign must be -1 (forward) or +1 (inverse)");
+  if (n >= ((i64)1 << 31)) return fail(AF_ERR_UNSUPPORTED, "size must be below 2^31");
+  af_plan_s* P = new af_plan_s();
+  try {
+    P->n = n;
+    P->sign = sign;
+    P->algo = algo;
+    P->root = plan_root(P->planner, n, algo);
+    P->p64 = af64::plan_create(n, sign, algo);
+    // build the batch-1 program now so that tables are generated at plan time
+    if (n > 0) af64::plan_launches(P->p64, 1);
+    check_cuda(cudaDeviceSynchronize(), "plan tables");
+  } catch (...) {
+    delete P;
+    throw;
+  }
+  *plan = P;
+  return AF_OK;
+  AF_CATCH
+}
+
+static af_status exec_sign_f64(af_plan plan, int sign, af_layout layout, const double* in_re, const double* in_im,
+                               double* out_re, double* out_im, int64_t batch, af_stream stream) {
+  AF_TRY
+  if (!plan) return fail(AF_ERR_INVALID, "null plan");
+  if (!plan->p64) return fail(AF_ERR_INVALID, "the plan is Complex Float: use the entry points without _f64");
+  if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
+  if (batch == 0 || plan->n == 0) return AF_OK;
+  if (layout != AF_LAYOUT_INTERLEAVED && layout != AF_LAYOUT_PLANAR) return fail(AF_ERR_INVALID, "bad layout");
+  if (!in_re || !out_re) return fail(AF_ERR_INVALID, "null data pointer");
+  const bool planar = layout == AF_LAYOUT_PLANAR;
+  if (planar && (!in_im || !out_im)) return fail(AF_ERR_INVALID, "planar layout needs im pointers");
+  if (!planar && (((uintptr_t)in_re | (uintptr_t)out_re) & 15))
+    return fail(AF_ERR_INVALID, "interleaved Complex Double data must be 16-byte aligned");
+  if (plan->n * batch >= ((i64)1 << 31)) return fail(AF_ERR_UNSUPPORTED, "n * batch must be below 2^31");
+  af64::plan_exec(plan->p64, sign, in_re, planar ? in_im : nullptr, out_re, planar ? out_im : nullptr, batch,
+                  (cudaStream_t)stream);
+  return AF_OK;
+  AF_CATCH
+}
+
+af_status af_exec_c2c_f64(af_plan plan, af_layout layout, const double* in_re, const double* in_im,
+                          double* out_re, double* out_im, int64_t batch, af_stream stream) {
+  if (!plan) return fail(AF_ERR_INVALID, "null plan");
+  return exec_sign_f64(plan, plan->sign, layout, in_re, in_im, out_re, out_im, batch, stream);
+}
+
+af_status af_vjp_c2c_f64(af_plan plan, af_layout layout, const double* cot_re, const double* cot_im,
+                         double* grad_re, double* grad_im, int64_t batch, af_stream stream) {
+  if (!plan) return fail(AF_ERR_INVALID, "null plan");
+  return exec_sign_f64(plan, -plan->sign, layout, cot_re, cot_im, grad_re, grad_im, batch, stream);
+}
+
 af_status af_plan_destroy(af_plan plan) {
   AF_TRY
   delete plan;
@@ -249,7 +314,9 @@ af_status af_plan_tree(int64_t n, af_algo algo, char* buf, size_t len) {
 af_status af_plan_launches(af_plan plan, int64_t batch, int64_t* launches) {
   AF_TRY
   if (!plan || !launches || batch < 0) return fail(AF_ERR_INVALID, "bad argument");
-  *launches = (batch == 0 || plan->n == 0) ? 0 : (int64_t)program_for(plan, batch, plan->sign).launches.size();
+  if (batch == 0 || plan->n == 0) *launches = 0;
+  else if (plan->p64) *launches = af64::plan_launches(plan->p64, batch);
+  else *launches = (int64_t)program_for(plan, batch, plan->sign).launches.size();
   return AF_OK;
   AF_CATCH
 }
@@ -393,7 +460,66 @@ static void run_nd(af_plan_s* const* plans, int dims, const float* in_re, const 
   }
 }
 
+// the multi-axis Complex Double transforms (same axis order as run_nd)
+static void run_nd_f64(af_plan_s* const* plans, int dims, const double* in_re, const double* in_im,
+                       double* out_re, double* out_im, i64 batch, cudaStream_t st) {
+  i64 total = batch;
+  for (int d = 0; d < dims; ++d) {
+    if (!plans[d]) throw AfError(AF_ERR_INVALID, "null plan");
+    if (!plans[d]->p64) throw AfError(AF_ERR_INVALID, "the plan is Complex Float: use the entry points without _f64");
+    total *= plans[d]->n;
+  }
+  if (total == 0) return;
+  if (total >= ((i64)1 << 31)) throw AfError(AF_ERR_UNSUPPORTED, "array must hold fewer than 2^31 values");
+  i64 inner = 1;
+  for (int d = 0; d < dims; ++d) {
+    const i64 outer = total / (inner * plans[d]->n);
+    if (d == 0) af64::plan_exec_axis(plans[d]->p64, in_re, in_im, out_re, out_im, outer, inner, st);
+    else af64::plan_exec_axis(plans[d]->p64, out_re, out_im, out_re, out_im, outer, inner, st);
+    inner *= plans[d]->n;
+  }
+}
+
+static void check_io_f64(af_layout layout, const double* a_re, const double* a_im, const double* b_re,
+                         const double* b_im) {
+  if (layout != AF_LAYOUT_INTERLEAVED && layout != AF_LAYOUT_PLANAR) throw AfError(AF_ERR_INVALID, "bad layout");
+  if (!a_re || !b_re) throw AfError(AF_ERR_INVALID, "null data pointer");
+  if (layout == AF_LAYOUT_PLANAR && (!a_im || !b_im)) throw AfError(AF_ERR_INVALID, "planar layout needs im pointers");
+  if (layout == AF_LAYOUT_INTERLEAVED && (((uintptr_t)a_re | (uintptr_t)b_re) & 15))
+    throw AfError(AF_ERR_INVALID, "interleaved Complex Double data must be 16-byte aligned");
+}
+
 extern "C" {
+
+af_status af_exec_c2c_2d_f64(af_plan plan0, af_plan plan1, af_layout layout, const double* in_re,
+                             const double* in_im, double* out_re, double* out_im, int64_t batch, af_stream stream) {
+  AF_TRY
+  if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
+  if (!plan0 || !plan1) return fail(AF_ERR_INVALID, "null plan");
+  af_plan_s* plans[2] = {plan0, plan1};
+  if (batch == 0 || plan0->n == 0 || plan1->n == 0) return AF_OK;
+  check_io_f64(layout, in_re, in_im, out_re, out_im);
+  const bool planar = layout == AF_LAYOUT_PLANAR;
+  run_nd_f64(plans, 2, in_re, planar ? in_im : nullptr, out_re, planar ? out_im : nullptr, batch,
+             (cudaStream_t)stream);
+  return AF_OK;
+  AF_CATCH
+}
+
+af_status af_exec_c2c_3d_f64(af_plan plan0, af_plan plan1, af_plan plan2, af_layout layout, const double* in_re,
+                             const double* in_im, double* out_re, double* out_im, int64_t batch, af_stream stream) {
+  AF_TRY
+  if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
+  if (!plan0 || !plan1 || !plan2) return fail(AF_ERR_INVALID, "null plan");
+  af_plan_s* plans[3] = {plan0, plan1, plan2};
+  if (batch == 0 || plan0->n == 0 || plan1->n == 0 || plan2->n == 0) return AF_OK;
+  check_io_f64(layout, in_re, in_im, out_re, out_im);
+  const bool planar = layout == AF_LAYOUT_PLANAR;
+  run_nd_f64(plans, 3, in_re, planar ? in_im : nullptr, out_re, planar ? out_im : nullptr, batch,
+             (cudaStream_t)stream);
+  return AF_OK;
+  AF_CATCH
+}
 
 af_status af_exec_c2c_axis(af_plan plan, af_layout layout, const float* in_re, const float* in_im, float* out_re,
                            float* out_im, int64_t outer, int64_t inner, af_stream stream) {

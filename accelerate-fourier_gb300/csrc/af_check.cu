@@ -14,7 +14,7 @@
 
 #include "af_host.h"
 
-namespace af {
+namespace AF_NS {
 
 const Program& batch_program(BatchPlan* B, int which);
 i64 batch_ws(BatchPlan* B);
@@ -216,23 +216,40 @@ static int report(const std::string& err, char* msg, size_t len) {
 
 }  // namespace af
 
-using namespace af;
+using namespace AF_NS;
+
+// the checker of the Complex Double engine exports the same entry points
+// with an _f64 suffix
+#ifdef AF_F64
+#define AFX(name) name##_f64
+#else
+#define AFX(name) name
+#endif
+
+// a plan without a device: reference tree and resources in dry mode
+struct DryPlan {
+  af::Planner planner;
+  PlanRes res;
+  const af::Node* root = nullptr;
+  i64 n = 0;
+  int sign = -1;
+};
 
 extern "C" {
 
 // Builds the programs of a plan (both signs) for `batch` rows without a
 // device and checks every address.  0: all in bounds and every output
 // element written once; 1: violation (msg); -1: the plan could not be built.
-int afx_check_plan(int64_t n, int sign, int algo, int64_t batch, char* msg, size_t len) {
+int AFX(afx_check_plan)(int64_t n, int sign, int algo, int64_t batch, char* msg, size_t len) {
   try {
-    af_plan_s P;
+    DryPlan P;
     P.res.dry = true;
     P.n = n;
     P.sign = sign;
     P.root = plan_root(P.planner, n, algo);
     for (int s : {sign, -sign}) {
       Program prog;
-      build_program(P.res, P.root, (float)s, batch, &prog);
+      build_program(P.res, P.root, (rl)s, batch, &prog);
       Checker c(P.res);
       c.where = s == sign ? "forward program" : "vjp program";
       c.sz[BUF_IN] = c.sz[BUF_OUT] = c.sz[BUF_AUX] = n * batch;
@@ -251,9 +268,9 @@ int afx_check_plan(int64_t n, int sign, int algo, int64_t batch, char* msg, size
 
 // The same for a transform along the middle axis of (outer, n, inner) arrays
 // (the programs behind af_exec_c2c_axis and the 2-D/3-D transforms).
-int afx_check_axis(int64_t n, int sign, int algo, int64_t outer, int64_t inner, char* msg, size_t len) {
+int AFX(afx_check_axis)(int64_t n, int sign, int algo, int64_t outer, int64_t inner, char* msg, size_t len) {
   try {
-    af_plan_s P;
+    DryPlan P;
     P.res.dry = true;
     P.n = n;
     P.sign = sign;
@@ -267,7 +284,7 @@ int afx_check_axis(int64_t n, int sign, int algo, int64_t outer, int64_t inner, 
     View out = in;
     out.buf = BUF_OUT;
     Program prog;
-    build_program_view(P.res, P.root, (float)sign, outer * inner, in, out, &prog);
+    build_program_view(P.res, P.root, (rl)sign, outer * inner, in, out, &prog);
     Checker c(P.res);
     c.where = "axis program";
     const i64 total = outer * n * inner;
@@ -285,7 +302,7 @@ int afx_check_axis(int64_t n, int sign, int algo, int64_t outer, int64_t inner, 
 }
 
 // The same for a batch of mixed lengths (forward, VJP and cotangent programs).
-int afx_check_batch(const int64_t* ns, int64_t count, int sign, char* msg, size_t len) {
+int AFX(afx_check_batch)(const int64_t* ns, int64_t count, int sign, char* msg, size_t len) {
   BatchPlan* B = nullptr;
   try {
     B = batch_create_mode((const i64*)ns, count, sign, true);
@@ -319,7 +336,7 @@ extern "C" {
 // Text summary of a batch program (which: 0 forward, 1 VJP, 2 cotangent),
 // built without a device: one line per launch with its type, threads, CTAs,
 // shared buffer size and the tile descriptors' kinds, lengths and maps.
-int afx_describe_batch(const int64_t* ns, int64_t count, int sign, int which, char* buf, size_t len) {
+int AFX(afx_describe_batch)(const int64_t* ns, int64_t count, int sign, int which, char* buf, size_t len) {
   BatchPlan* B = nullptr;
   try {
     B = batch_create_mode((const i64*)ns, count, sign, true);

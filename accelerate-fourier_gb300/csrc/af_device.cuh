@@ -9,6 +9,35 @@
 #define AF_MAXPH 2      // max FFT phases in one tile program
 #define AF_HD __host__ __device__ __forceinline__
 
+// Element precision of the engine.  The engine (descriptors, kernels,
+// lowering, executor) compiles twice: Complex Float in namespace af, and with
+// AF_F64 defined, Complex Double in namespace af64.  The reference transforms
+// are polymorphic over the element type (A.RealFloat a,
+// src/Data/Array/Accelerate/Fourier/Planned.hs:103-106).
+#ifdef AF_F64
+#define AF_NS af64
+#else
+#define AF_NS af
+#endif
+
+namespace af {}
+namespace AF_NS {
+#ifdef AF_F64
+using namespace af;  // the planner and error types are shared by both precisions
+#endif
+
+#ifdef AF_F64
+typedef double2 cx;
+typedef double rl;
+AF_HD cx make_cx(rl x, rl y) { return make_double2(x, y); }
+AF_HD rl rfma(rl a, rl b, rl c) { return fma(a, b, c); }
+#else
+typedef float2 cx;
+typedef float rl;
+AF_HD cx make_cx(rl x, rl y) { return make_float2(x, y); }
+AF_HD rl rfma(rl a, rl b, rl c) { return fmaf(a, b, c); }
+#endif
+
 typedef long long i64;
 
 // ---------------------------------------------------------------- fast divide
@@ -65,28 +94,28 @@ __device__ __forceinline__ unsigned mulmod(unsigned a, unsigned b, const ModN& M
 
 // ---------------------------------------------------------------- complex ops
 // Complex add and subtract use the packed two-lane FP32 add of sm_100+
-// (one instruction for both parts) in device code.
-AF_HD float2 cadd(float2 a, float2 b) {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+// (one instruction for both parts) in FP32 device code.
+AF_HD cx cadd(cx a, cx b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(AF_F64)
   return __fadd2_rn(a, b);
 #else
-  return make_float2(a.x + b.x, a.y + b.y);
+  return make_cx(a.x + b.x, a.y + b.y);
 #endif
 }
-AF_HD float2 csub(float2 a, float2 b) {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+AF_HD cx csub(cx a, cx b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(AF_F64)
+  return __fadd2_rn(a, make_cx(-b.x, -b.y));
 #else
-  return make_float2(a.x - b.x, a.y - b.y);
+  return make_cx(a.x - b.x, a.y - b.y);
 #endif
 }
-AF_HD float2 cmul(float2 a, float2 b) {
-  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+AF_HD cx cmul(cx a, cx b) {
+  return make_cx(rfma(a.x, b.x, -a.y * b.y), rfma(a.x, b.y, a.y * b.x));
 }
-AF_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-AF_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+AF_HD cx cscale(cx a, rl s) { return make_cx(a.x * s, a.y * s); }
+AF_HD cx conjf2(cx a) { return make_cx(a.x, -a.y); }
 // multiply by sign*i  (sign = +-1):  (sign*i)(x+iy) = sign*(-y + ix)
-AF_HD float2 mul_si(float2 a, float sign) { return make_float2(-sign * a.y, sign * a.x); }
+AF_HD cx mul_si(cx a, rl sign) { return make_cx(-sign * a.y, sign * a.x); }
 
 // ---------------------------------------------------------------- descriptors
 // One Stockham pass of radix R over a phase of length n: the pass reads
@@ -104,7 +133,7 @@ struct PassDesc {
 // elements are es apart (positions before bank padding).
 struct FftPhase {
   int n, npass, ls, es, lcnt;
-  float sign;
+  rl sign;
   int tw_off;      // offset of this phase's tables in the shared table area
   int twS_log2;    // two-level table split S = 1<<twS_log2 (lo table S, hi table H)
   FastDiv lcnt_div;
@@ -115,9 +144,9 @@ struct FftPhase {
 // passes their base pointers (interleaved `c`, or planar `re`/`im` planes).
 enum BufId { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_AUX = 3, BUF_COUNT = 4 };
 struct TileBases {
-  float2* c[BUF_COUNT];
-  float* re[BUF_COUNT];
-  float* im[BUF_COUNT];
+  cx* c[BUF_COUNT];
+  rl* re[BUF_COUNT];
+  rl* im[BUF_COUNT];
 };
 
 // Index maps of one side of a tile (element e of a line with lo index `lo`).
@@ -144,7 +173,7 @@ struct IoDesc {
   ModN m_mod;       // IO_GT: reduction mod mN (constants mA, mB reduced mod mN)
   i64 s_t;          // element stride of a mapped transform
   const int* tab;
-  const float2* vec;
+  const cx* vec;
   i64 x0_off, x0_shi;  // IO_RADER: x0 at x0_off + hi*x0_shi in buffer x0_buf
   i64 dc_off;          // IO_RADER: DC of transform hi at ws[dc_off + hi]
   const i64* loff;     // AFFINE views: when set, line l starts at loff[l] (gathered lines)
@@ -165,17 +194,17 @@ struct TileDesc {
   int nlines;        // total lines of the step (all CTAs)
   int LS;            // shared-memory stride between lines (unpadded units)
   int slen;          // elements per line held in shared memory (M for conv tiles)
-  int tw_total;      // float2 table entries staged in shared memory
+  int tw_total;      // cx table entries staged in shared memory
   int nph;
-  const float2* tw_src;  // table source (device)
+  const cx* tw_src;  // table source (device)
   FftPhase ph[AF_MAXPH];
   FastDiv N_div, S_div, G_div;  // nlen, slen, G
   IoDesc in, out;
-  float scale;       // multiplies every stored element
-  float ptw_sign;
+  rl scale;       // multiplies every stored element
+  rl ptw_sign;
   // four-step twiddle on store: element e of a line with lo index c is
   // multiplied by W_N^(c*e) (two-level table: S lo entries then hi entries)
-  const float2* ptw;
+  const cx* ptw;
   int ptwS_log2;
   int cot;           // 1: store g = 2 w v (w read from BUF_AUX at the output
                      // address) and add w |v|^2 to the loss
@@ -188,8 +217,8 @@ struct TileDesc {
   // Rader: dlog[r-1] = log_g(r) for r = 1..p-1
   const int* dlog;
   // Bluestein chirp (N entries); conv spectrum (Rader zs / chirp spectrum / S)
-  const float2* vec_a;
-  const float2* vec_b;
+  const cx* vec_a;
+  const cx* vec_b;
   // TILE_CONVROW: spectrum index q = lo*sq_lo + e*sq_e; DC of line lo == 0,
   // element 0 after the first FFT goes to ws[dc_off + hi] (dc_off < 0: none)
   i64 sq_lo, sq_e, dc_off;
@@ -210,17 +239,17 @@ struct WorkItem {
 };
 
 // ---------------------------------------------------------------- smem layout
-// One padding slot every 2^sh float2 keeps strided Stockham accesses off bank
+// One padding slot every 2^sh cx keeps strided Stockham accesses off bank
 // conflicts; each tile picks sh (sh = 31: no padding).
 __device__ __forceinline__ int spd_(int i, int sh) { return i + (i >> sh); }
 
 // ---------------------------------------------------------------- twiddles
 // Tables hold the forward root: tab[t] = exp(-2*pi*i*t/n), as two levels
 // lo[t & (S-1)] * hi[t >> log2 S].  sign > 0 conjugates.
-__device__ __forceinline__ float2 tw_lookup(const float2* tab, int S_log2, int t, float sign) {
-  float2 lo = tab[t & ((1 << S_log2) - 1)];
-  float2 hi = tab[(1 << S_log2) + (t >> S_log2)];
-  float2 w = cmul(hi, lo);
+__device__ __forceinline__ cx tw_lookup(const cx* tab, int S_log2, int t, rl sign) {
+  cx lo = tab[t & ((1 << S_log2) - 1)];
+  cx hi = tab[(1 << S_log2) + (t >> S_log2)];
+  cx w = cmul(hi, lo);
   w.y *= -sign;  // forward (sign=-1) keeps the stored root
   return w;
 }
@@ -230,16 +259,16 @@ __device__ __forceinline__ float2 tw_lookup(const float2* tab, int S_log2, int t
 template <int R> struct Dft;
 
 template <> struct Dft<2> {
-  static __device__ __forceinline__ void run(float2* u, float, const float2*, int, int) {
-    float2 a = u[0], b = u[1];
+  static __device__ __forceinline__ void run(cx* u, rl, const cx*, int, int) {
+    cx a = u[0], b = u[1];
     u[0] = cadd(a, b);
     u[1] = csub(a, b);
   }
 };
 
-__device__ __forceinline__ void dft4(float2& u0, float2& u1, float2& u2, float2& u3, float sign) {
-  float2 t0 = cadd(u0, u2), t1 = csub(u0, u2);
-  float2 t2 = cadd(u1, u3), t3 = mul_si(csub(u1, u3), sign);
+__device__ __forceinline__ void dft4(cx& u0, cx& u1, cx& u2, cx& u3, rl sign) {
+  cx t0 = cadd(u0, u2), t1 = csub(u0, u2);
+  cx t2 = cadd(u1, u3), t3 = mul_si(csub(u1, u3), sign);
   u0 = cadd(t0, t2);
   u2 = csub(t0, t2);
   u1 = cadd(t1, t3);
@@ -247,32 +276,32 @@ __device__ __forceinline__ void dft4(float2& u0, float2& u1, float2& u2, float2&
 }
 
 template <> struct Dft<4> {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
     dft4(u[0], u[1], u[2], u[3], sign);
   }
 };
 
-#define AF_R2 0.70710678118654752440f
-#define AF_C8 0.92387953251128675613f
-#define AF_S8 0.38268343236508977173f
+#define AF_R2 ((rl)0.70710678118654752440)
+#define AF_C8 ((rl)0.92387953251128675613)
+#define AF_S8 ((rl)0.38268343236508977173)
 
 // multiply by w8^m = exp(sign*2*pi*i*m/8)
-__device__ __forceinline__ float2 mul_w8(float2 a, int m, float sign) {
+__device__ __forceinline__ cx mul_w8(cx a, int m, rl sign) {
   switch (m & 7) {
     case 0: return a;
-    case 1: return cmul(a, make_float2(AF_R2, sign * AF_R2));
+    case 1: return cmul(a, make_cx(AF_R2, sign * AF_R2));
     case 2: return mul_si(a, sign);
-    case 3: return cmul(a, make_float2(-AF_R2, sign * AF_R2));
-    case 4: return make_float2(-a.x, -a.y);
-    case 5: return cmul(a, make_float2(-AF_R2, -sign * AF_R2));
+    case 3: return cmul(a, make_cx(-AF_R2, sign * AF_R2));
+    case 4: return make_cx(-a.x, -a.y);
+    case 5: return cmul(a, make_cx(-AF_R2, -sign * AF_R2));
     case 6: return mul_si(a, -sign);
-    default: return cmul(a, make_float2(AF_R2, -sign * AF_R2));
+    default: return cmul(a, make_cx(AF_R2, -sign * AF_R2));
   }
 }
 
 template <> struct Dft<8> {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
-    float2 a[4], b[4];
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+    cx a[4], b[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       a[j] = cadd(u[j], u[j + 4]);
@@ -286,21 +315,21 @@ template <> struct Dft<8> {
 };
 
 // multiply by w16^m, m in 0..9
-__device__ __forceinline__ float2 mul_w16(float2 a, int m, float sign) {
+__device__ __forceinline__ cx mul_w16(cx a, int m, rl sign) {
   switch (m) {
     case 0: return a;
-    case 1: return cmul(a, make_float2(AF_C8, sign * AF_S8));
+    case 1: return cmul(a, make_cx(AF_C8, sign * AF_S8));
     case 2: return mul_w8(a, 1, sign);
-    case 3: return cmul(a, make_float2(AF_S8, sign * AF_C8));
+    case 3: return cmul(a, make_cx(AF_S8, sign * AF_C8));
     case 4: return mul_w8(a, 2, sign);
     case 6: return mul_w8(a, 3, sign);
-    case 9: return cmul(a, make_float2(-AF_C8, -sign * AF_S8));
+    case 9: return cmul(a, make_cx(-AF_C8, -sign * AF_S8));
     default: return a;  // unused
   }
 }
 
 template <> struct Dft<16> {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
     // 4 x 4: v_a = DFT4(u[a + 4m]); v_a[b] *= w16^(a b); y[b + 4c] = DFT4_a(v_a[b])
 #pragma unroll
     for (int a = 0; a < 4; ++a) dft4(u[a], u[a + 4], u[a + 8], u[a + 12], sign);
@@ -308,10 +337,10 @@ template <> struct Dft<16> {
     for (int a = 1; a < 4; ++a)
 #pragma unroll
       for (int b = 1; b < 4; ++b) u[a + 4 * b] = mul_w16(u[a + 4 * b], a * b, sign);
-    float2 t[16];
+    cx t[16];
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      float2 x0 = u[0 + 4 * b], x1 = u[1 + 4 * b], x2 = u[2 + 4 * b], x3 = u[3 + 4 * b];
+      cx x0 = u[0 + 4 * b], x1 = u[1 + 4 * b], x2 = u[2 + 4 * b], x3 = u[3 + 4 * b];
       dft4(x0, x1, x2, x3, sign);
       t[b] = x0; t[b + 4] = x1; t[b + 8] = x2; t[b + 12] = x3;
     }
@@ -321,12 +350,12 @@ template <> struct Dft<16> {
 };
 
 template <> struct Dft<3> {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
-    const float c = -0.5f, s = 0.86602540378443864676f * sign;
-    float2 t = cadd(u[1], u[2]);
-    float2 d = csub(u[1], u[2]);
-    float2 m = make_float2(fmaf(c, t.x, u[0].x), fmaf(c, t.y, u[0].y));
-    float2 r = make_float2(-s * d.y, s * d.x);
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+    const rl c = (rl)-0.5, s = (rl)0.86602540378443864676 * sign;
+    cx t = cadd(u[1], u[2]);
+    cx d = csub(u[1], u[2]);
+    cx m = make_cx(rfma(c, t.x, u[0].x), rfma(c, t.y, u[0].y));
+    cx r = make_cx(-s * d.y, s * d.x);
     u[0] = cadd(u[0], t);
     u[1] = cadd(m, r);
     u[2] = csub(m, r);
@@ -334,16 +363,16 @@ template <> struct Dft<3> {
 };
 
 template <> struct Dft<5> {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
-    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
-    const float s1 = 0.95105651629515357212f * sign, s2 = 0.58778525229247312917f * sign;
-    float2 p1 = cadd(u[1], u[4]), m1 = csub(u[1], u[4]);
-    float2 p2 = cadd(u[2], u[3]), m2 = csub(u[2], u[3]);
-    float2 a1 = make_float2(u[0].x + c1 * p1.x + c2 * p2.x, u[0].y + c1 * p1.y + c2 * p2.y);
-    float2 a2 = make_float2(u[0].x + c2 * p1.x + c1 * p2.x, u[0].y + c2 * p1.y + c1 * p2.y);
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+    const rl c1 = (rl)0.30901699437494742410, c2 = (rl)-0.80901699437494742410;
+    const rl s1 = (rl)0.95105651629515357212 * sign, s2 = (rl)0.58778525229247312917 * sign;
+    cx p1 = cadd(u[1], u[4]), m1 = csub(u[1], u[4]);
+    cx p2 = cadd(u[2], u[3]), m2 = csub(u[2], u[3]);
+    cx a1 = make_cx(u[0].x + c1 * p1.x + c2 * p2.x, u[0].y + c1 * p1.y + c2 * p2.y);
+    cx a2 = make_cx(u[0].x + c2 * p1.x + c1 * p2.x, u[0].y + c2 * p1.y + c1 * p2.y);
     // b = i*(s1 m1 + s2 m2), c = i*(s2 m1 - s1 m2)
-    float2 b1 = make_float2(-(s1 * m1.y + s2 * m2.y), s1 * m1.x + s2 * m2.x);
-    float2 b2 = make_float2(-(s2 * m1.y - s1 * m2.y), s2 * m1.x - s1 * m2.x);
+    cx b1 = make_cx(-(s1 * m1.y + s2 * m2.y), s1 * m1.x + s2 * m2.x);
+    cx b2 = make_cx(-(s2 * m1.y - s1 * m2.y), s2 * m1.x - s1 * m2.x);
     u[0] = cadd(u[0], cadd(p1, p2));
     u[1] = cadd(a1, b1);
     u[4] = csub(a1, b1);
@@ -354,71 +383,71 @@ template <> struct Dft<5> {
 
 // Odd prime radix (7, 11, 13): symmetric direct DFT with the constants
 // cos(2 pi m/R), sin(2 pi m/R), m <= (R-1)/2 (computed in double precision
-// and rounded to float).
+// and rounded to rl).
 template <int R> struct OddRoots;
 template <> struct OddRoots<7> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[4] = {1.0f, 0.62348980185873359439f, -0.22252093395631433737f, -0.90096886790241903498f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[4] = {1.0f, 0.62348980185873359439, -0.22252093395631433737, -0.90096886790241903498};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[4] = {0.0f, 0.78183148246802980363f, 0.97492791218182361934f, 0.43388373911755823142f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[4] = {0.0f, 0.78183148246802980363, 0.97492791218182361934, 0.43388373911755823142};
     return v[m];
   }
 };
 template <> struct OddRoots<11> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[6] = {1.0f, 0.84125353283118120551f, 0.41541501300188643508f, -0.14231483827328500480f,
-                            -0.65486073394528498959f, -0.95949297361449736865f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[6] = {1.0f, 0.84125353283118120551, 0.41541501300188643508, -0.14231483827328500480,
+                            -0.65486073394528498959, -0.95949297361449736865};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[6] = {0.0f, 0.54064081745559755543f, 0.90963199535451833011f, 0.98982144188093279524f,
-                            0.75574957435425826890f, 0.28173255684142967104f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[6] = {0.0f, 0.54064081745559755543, 0.90963199535451833011, 0.98982144188093279524,
+                            0.75574957435425826890, 0.28173255684142967104};
     return v[m];
   }
 };
 template <> struct OddRoots<13> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[7] = {1.0f, 0.88545602565320991051f, 0.56806474673115592289f, 0.12053668025532300601f,
-                            -0.35460488704253545489f, -0.74851074817110119231f, -0.97094181742605201180f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[7] = {1.0f, 0.88545602565320991051, 0.56806474673115592289, 0.12053668025532300601,
+                            -0.35460488704253545489, -0.74851074817110119231, -0.97094181742605201180};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[7] = {0.0f, 0.46472317204376850652f, 0.82298386589365635224f, 0.99270887409805397272f,
-                            0.93501624268541483342f, 0.66312265824079519305f, 0.23931566428755768339f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[7] = {0.0f, 0.46472317204376850652, 0.82298386589365635224, 0.99270887409805397272,
+                            0.93501624268541483342, 0.66312265824079519305, 0.23931566428755768339};
     return v[m];
   }
 };
 
 template <int R> struct DftOdd {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2*, int, int) {
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
     constexpr int h = (R - 1) / 2;
-    float2 P[h + 1], M[h + 1];
-    float2 y0 = u[0];
+    cx P[h + 1], M[h + 1];
+    cx y0 = u[0];
 #pragma unroll
     for (int j = 1; j <= h; ++j) {
       P[j] = cadd(u[j], u[R - j]);
       M[j] = csub(u[j], u[R - j]);
       y0 = cadd(y0, P[j]);
     }
-    float2 out[R];
+    cx out[R];
     out[0] = y0;
 #pragma unroll
     for (int k = 1; k <= h; ++k) {
-      float2 a = u[0], b = make_float2(0.f, 0.f);
+      cx a = u[0], b = make_cx(0.f, 0.f);
 #pragma unroll
       for (int j = 1; j <= h; ++j) {
         // cos/sin of 2 pi (j k mod R)/R from the first half (symmetry)
         const int m = (j * k) % R;
-        const float cm = OddRoots<R>::c(m <= h ? m : R - m);
-        const float sm = m <= h ? OddRoots<R>::s(m) : -OddRoots<R>::s(R - m);
-        a.x = fmaf(cm, P[j].x, a.x);
-        a.y = fmaf(cm, P[j].y, a.y);
-        b.x = fmaf(sm, M[j].x, b.x);
-        b.y = fmaf(sm, M[j].y, b.y);
+        const rl cm = OddRoots<R>::c(m <= h ? m : R - m);
+        const rl sm = m <= h ? OddRoots<R>::s(m) : -OddRoots<R>::s(R - m);
+        a.x = rfma(cm, P[j].x, a.x);
+        a.y = rfma(cm, P[j].y, a.y);
+        b.x = rfma(sm, M[j].x, b.x);
+        b.y = rfma(sm, M[j].y, b.y);
       }
-      float2 ib = mul_si(b, sign);
+      cx ib = mul_si(b, sign);
       out[k] = cadd(a, ib);
       out[R - k] = csub(a, ib);
     }
@@ -432,120 +461,120 @@ template <> struct Dft<13> : DftOdd<13> {};
 
 // Roots of unity for the composite radices: Roots<R>::c(m) = cos(2 pi m/R),
 // Roots<R>::s(m) = sin(2 pi m/R), m < R (computed in double precision and
-// rounded to float).
+// rounded to rl).
 template <int R> struct Roots;
 template <> struct Roots<6> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[6] = {1.00000000000000000000e+00f, 5.00000000000000111022e-01f, -4.99999999999999777955e-01f, -1.00000000000000000000e+00f, -5.00000000000000444089e-01f, 5.00000000000000111022e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[6] = {1.00000000000000000000e+00, 5.00000000000000111022e-01, -4.99999999999999777955e-01, -1.00000000000000000000e+00, -5.00000000000000444089e-01, 5.00000000000000111022e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[6] = {0.00000000000000000000e+00f, 8.66025403784438596588e-01f, 8.66025403784438707611e-01f, 0.00000000000000000000e+00f, -8.66025403784438374544e-01f, -8.66025403784438596588e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[6] = {0.00000000000000000000e+00, 8.66025403784438596588e-01, 8.66025403784438707611e-01, 0.00000000000000000000e+00, -8.66025403784438374544e-01, -8.66025403784438596588e-01};
     return v[m];
   }
 };
 template <> struct Roots<9> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[9] = {1.00000000000000000000e+00f, 7.66044443118978013452e-01f, 1.73648177666930414453e-01f, -4.99999999999999777955e-01f, -9.39692620785908316883e-01f, -9.39692620785908427905e-01f, -5.00000000000000444089e-01f, 1.73648177666929970364e-01f, 7.66044443118977791407e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[9] = {1.00000000000000000000e+00, 7.66044443118978013452e-01, 1.73648177666930414453e-01, -4.99999999999999777955e-01, -9.39692620785908316883e-01, -9.39692620785908427905e-01, -5.00000000000000444089e-01, 1.73648177666929970364e-01, 7.66044443118977791407e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[9] = {0.00000000000000000000e+00f, 6.42787609686539251896e-01f, 9.84807753012208020316e-01f, 8.66025403784438707611e-01f, 3.42020143325668879442e-01f, -3.42020143325668657397e-01f, -8.66025403784438374544e-01f, -9.84807753012208131338e-01f, -6.42787609686539584963e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[9] = {0.00000000000000000000e+00, 6.42787609686539251896e-01, 9.84807753012208020316e-01, 8.66025403784438707611e-01, 3.42020143325668879442e-01, -3.42020143325668657397e-01, -8.66025403784438374544e-01, -9.84807753012208131338e-01, -6.42787609686539584963e-01};
     return v[m];
   }
 };
 template <> struct Roots<10> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[10] = {1.00000000000000000000e+00f, 8.09016994374947451263e-01f, 3.09016994374947451263e-01f, -3.09016994374947340241e-01f, -8.09016994374947340241e-01f, -1.00000000000000000000e+00f, -8.09016994374947562285e-01f, -3.09016994374947562285e-01f, 3.09016994374947229218e-01f, 8.09016994374947340241e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[10] = {1.00000000000000000000e+00, 8.09016994374947451263e-01, 3.09016994374947451263e-01, -3.09016994374947340241e-01, -8.09016994374947340241e-01, -1.00000000000000000000e+00, -8.09016994374947562285e-01, -3.09016994374947562285e-01, 3.09016994374947229218e-01, 8.09016994374947340241e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[10] = {0.00000000000000000000e+00f, 5.87785252292473137103e-01f, 9.51056516295153531182e-01f, 9.51056516295153642204e-01f, 5.87785252292473248126e-01f, 0.00000000000000000000e+00f, -5.87785252292473026081e-01f, -9.51056516295153531182e-01f, -9.51056516295153642204e-01f, -5.87785252292473359148e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[10] = {0.00000000000000000000e+00, 5.87785252292473137103e-01, 9.51056516295153531182e-01, 9.51056516295153642204e-01, 5.87785252292473248126e-01, 0.00000000000000000000e+00, -5.87785252292473026081e-01, -9.51056516295153531182e-01, -9.51056516295153642204e-01, -5.87785252292473359148e-01};
     return v[m];
   }
 };
 template <> struct Roots<12> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[12] = {1.00000000000000000000e+00f, 8.66025403784438707611e-01f, 5.00000000000000111022e-01f, 0.00000000000000000000e+00f, -4.99999999999999777955e-01f, -8.66025403784438707611e-01f, -1.00000000000000000000e+00f, -8.66025403784438818633e-01f, -5.00000000000000444089e-01f, 0.00000000000000000000e+00f, 5.00000000000000111022e-01f, 8.66025403784438374544e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[12] = {1.00000000000000000000e+00, 8.66025403784438707611e-01, 5.00000000000000111022e-01, 0.00000000000000000000e+00, -4.99999999999999777955e-01, -8.66025403784438707611e-01, -1.00000000000000000000e+00, -8.66025403784438818633e-01, -5.00000000000000444089e-01, 0.00000000000000000000e+00, 5.00000000000000111022e-01, 8.66025403784438374544e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[12] = {0.00000000000000000000e+00f, 4.99999999999999944489e-01f, 8.66025403784438596588e-01f, 1.00000000000000000000e+00f, 8.66025403784438707611e-01f, 4.99999999999999944489e-01f, 0.00000000000000000000e+00f, -4.99999999999999722444e-01f, -8.66025403784438374544e-01f, -1.00000000000000000000e+00f, -8.66025403784438596588e-01f, -5.00000000000000444089e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[12] = {0.00000000000000000000e+00, 4.99999999999999944489e-01, 8.66025403784438596588e-01, 1.00000000000000000000e+00, 8.66025403784438707611e-01, 4.99999999999999944489e-01, 0.00000000000000000000e+00, -4.99999999999999722444e-01, -8.66025403784438374544e-01, -1.00000000000000000000e+00, -8.66025403784438596588e-01, -5.00000000000000444089e-01};
     return v[m];
   }
 };
 template <> struct Roots<15> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[15] = {1.00000000000000000000e+00f, 9.13545457642600866599e-01f, 6.69130606358858237570e-01f, 3.09016994374947451263e-01f, -1.04528463267653332069e-01f, -4.99999999999999777955e-01f, -8.09016994374947340241e-01f, -9.78147600733805688833e-01f, -9.78147600733805688833e-01f, -8.09016994374947562285e-01f, -5.00000000000000444089e-01f, -1.04528463267654234126e-01f, 3.09016994374947229218e-01f, 6.69130606358858459615e-01f, 9.13545457642600977621e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[15] = {1.00000000000000000000e+00, 9.13545457642600866599e-01, 6.69130606358858237570e-01, 3.09016994374947451263e-01, -1.04528463267653332069e-01, -4.99999999999999777955e-01, -8.09016994374947340241e-01, -9.78147600733805688833e-01, -9.78147600733805688833e-01, -8.09016994374947562285e-01, -5.00000000000000444089e-01, -1.04528463267654234126e-01, 3.09016994374947229218e-01, 6.69130606358858459615e-01, 9.13545457642600977621e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[15] = {0.00000000000000000000e+00f, 4.06736643075800152758e-01f, 7.43144825477394133095e-01f, 9.51056516295153531182e-01f, 9.94521895368273400884e-01f, 8.66025403784438707611e-01f, 5.87785252292473248126e-01f, 2.07911690817759314820e-01f, -2.07911690817759065020e-01f, -5.87785252292473026081e-01f, -8.66025403784438374544e-01f, -9.94521895368273289861e-01f, -9.51056516295153642204e-01f, -7.43144825477394022073e-01f, -4.06736643075800152758e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[15] = {0.00000000000000000000e+00, 4.06736643075800152758e-01, 7.43144825477394133095e-01, 9.51056516295153531182e-01, 9.94521895368273400884e-01, 8.66025403784438707611e-01, 5.87785252292473248126e-01, 2.07911690817759314820e-01, -2.07911690817759065020e-01, -5.87785252292473026081e-01, -8.66025403784438374544e-01, -9.94521895368273289861e-01, -9.51056516295153642204e-01, -7.43144825477394022073e-01, -4.06736643075800152758e-01};
     return v[m];
   }
 };
 template <> struct Roots<20> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[20] = {1.00000000000000000000e+00f, 9.51056516295153531182e-01f, 8.09016994374947451263e-01f, 5.87785252292473137103e-01f, 3.09016994374947451263e-01f, 0.00000000000000000000e+00f, -3.09016994374947340241e-01f, -5.87785252292473026081e-01f, -8.09016994374947340241e-01f, -9.51056516295153531182e-01f, -1.00000000000000000000e+00f, -9.51056516295153753227e-01f, -8.09016994374947562285e-01f, -5.87785252292473248126e-01f, -3.09016994374947562285e-01f, 0.00000000000000000000e+00f, 3.09016994374947229218e-01f, 5.87785252292472915059e-01f, 8.09016994374947340241e-01f, 9.51056516295153531182e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[20] = {1.00000000000000000000e+00, 9.51056516295153531182e-01, 8.09016994374947451263e-01, 5.87785252292473137103e-01, 3.09016994374947451263e-01, 0.00000000000000000000e+00, -3.09016994374947340241e-01, -5.87785252292473026081e-01, -8.09016994374947340241e-01, -9.51056516295153531182e-01, -1.00000000000000000000e+00, -9.51056516295153753227e-01, -8.09016994374947562285e-01, -5.87785252292473248126e-01, -3.09016994374947562285e-01, 0.00000000000000000000e+00, 3.09016994374947229218e-01, 5.87785252292472915059e-01, 8.09016994374947340241e-01, 9.51056516295153531182e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[20] = {0.00000000000000000000e+00f, 3.09016994374947395752e-01f, 5.87785252292473137103e-01f, 8.09016994374947451263e-01f, 9.51056516295153531182e-01f, 1.00000000000000000000e+00f, 9.51056516295153642204e-01f, 8.09016994374947451263e-01f, 5.87785252292473248126e-01f, 3.09016994374947506774e-01f, 0.00000000000000000000e+00f, -3.09016994374946896151e-01f, -5.87785252292473026081e-01f, -8.09016994374947340241e-01f, -9.51056516295153531182e-01f, -1.00000000000000000000e+00f, -9.51056516295153642204e-01f, -8.09016994374947562285e-01f, -5.87785252292473359148e-01f, -3.09016994374947617796e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[20] = {0.00000000000000000000e+00, 3.09016994374947395752e-01, 5.87785252292473137103e-01, 8.09016994374947451263e-01, 9.51056516295153531182e-01, 1.00000000000000000000e+00, 9.51056516295153642204e-01, 8.09016994374947451263e-01, 5.87785252292473248126e-01, 3.09016994374947506774e-01, 0.00000000000000000000e+00, -3.09016994374946896151e-01, -5.87785252292473026081e-01, -8.09016994374947340241e-01, -9.51056516295153531182e-01, -1.00000000000000000000e+00, -9.51056516295153642204e-01, -8.09016994374947562285e-01, -5.87785252292473359148e-01, -3.09016994374947617796e-01};
     return v[m];
   }
 };
 template <> struct Roots<25> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[25] = {1.00000000000000000000e+00f, 9.68583161128631076053e-01f, 8.76306680043863583940e-01f, 7.28968627421411552447e-01f, 5.35826794978996545638e-01f, 3.09016994374947451263e-01f, 6.27905195293135265366e-02f, -1.87381314585724600974e-01f, -4.25779291565072715020e-01f, -6.37423989748689745483e-01f, -8.09016994374947340241e-01f, -9.29776485888251347234e-01f, -9.92114701314477764882e-01f, -9.92114701314477875904e-01f, -9.29776485888251458256e-01f, -8.09016994374947784330e-01f, -6.37423989748689523438e-01f, -4.25779291565072159909e-01f, -1.87381314585724628730e-01f, 6.27905195293128326472e-02f, 3.09016994374947229218e-01f, 5.35826794978996767682e-01f, 7.28968627421411219380e-01f, 8.76306680043863139851e-01f, 9.68583161128630965031e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[25] = {1.00000000000000000000e+00, 9.68583161128631076053e-01, 8.76306680043863583940e-01, 7.28968627421411552447e-01, 5.35826794978996545638e-01, 3.09016994374947451263e-01, 6.27905195293135265366e-02, -1.87381314585724600974e-01, -4.25779291565072715020e-01, -6.37423989748689745483e-01, -8.09016994374947340241e-01, -9.29776485888251347234e-01, -9.92114701314477764882e-01, -9.92114701314477875904e-01, -9.29776485888251458256e-01, -8.09016994374947784330e-01, -6.37423989748689523438e-01, -4.25779291565072159909e-01, -1.87381314585724628730e-01, 6.27905195293128326472e-02, 3.09016994374947229218e-01, 5.35826794978996767682e-01, 7.28968627421411219380e-01, 8.76306680043863139851e-01, 9.68583161128630965031e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[25] = {0.00000000000000000000e+00f, 2.48689887164854794843e-01f, 4.81753674101715323452e-01f, 6.84547105928688615073e-01f, 8.44327925502015075310e-01f, 9.51056516295153531182e-01f, 9.98026728428271558968e-01f, 9.82287250728688721146e-01f, 9.04827052466019465804e-01f, 7.70513242775789253258e-01f, 5.87785252292473248126e-01f, 3.68124552684678141290e-01f, 1.25333233564304535879e-01f, -1.25333233564304286078e-01f, -3.68124552684677919245e-01f, -5.87785252292472693014e-01f, -7.70513242775789364281e-01f, -9.04827052466019798871e-01f, -9.82287250728688721146e-01f, -9.98026728428271558968e-01f, -9.51056516295153642204e-01f, -8.44327925502014964287e-01f, -6.84547105928688948140e-01f, -4.81753674101716100608e-01f, -2.48689887164855349955e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[25] = {0.00000000000000000000e+00, 2.48689887164854794843e-01, 4.81753674101715323452e-01, 6.84547105928688615073e-01, 8.44327925502015075310e-01, 9.51056516295153531182e-01, 9.98026728428271558968e-01, 9.82287250728688721146e-01, 9.04827052466019465804e-01, 7.70513242775789253258e-01, 5.87785252292473248126e-01, 3.68124552684678141290e-01, 1.25333233564304535879e-01, -1.25333233564304286078e-01, -3.68124552684677919245e-01, -5.87785252292472693014e-01, -7.70513242775789364281e-01, -9.04827052466019798871e-01, -9.82287250728688721146e-01, -9.98026728428271558968e-01, -9.51056516295153642204e-01, -8.44327925502014964287e-01, -6.84547105928688948140e-01, -4.81753674101716100608e-01, -2.48689887164855349955e-01};
     return v[m];
   }
 };
 template <> struct Roots<27> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[27] = {1.00000000000000000000e+00f, 9.73044870579823806267e-01f, 8.93632640323412275052e-01f, 7.66044443118978013452e-01f, 5.97158591702786178956e-01f, 3.96079766039156899726e-01f, 1.73648177666930414453e-01f, -5.81448289104757737311e-02f, -2.86803232711090205775e-01f, -4.99999999999999777955e-01f, -6.86241637868733489469e-01f, -8.35487811412936265398e-01f, -9.39692620785908316883e-01f, -9.93238357741943023171e-01f, -9.93238357741943023171e-01f, -9.39692620785908538927e-01f, -8.35487811412936487443e-01f, -6.86241637868733600492e-01f, -5.00000000000000444089e-01f, -2.86803232711090649865e-01f, -5.81448289104762386370e-02f, 1.73648177666930830787e-01f, 3.96079766039156511148e-01f, 5.97158591702785845889e-01f, 7.66044443118977791407e-01f, 8.93632640323412164030e-01f, 9.73044870579824028312e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[27] = {1.00000000000000000000e+00, 9.73044870579823806267e-01, 8.93632640323412275052e-01, 7.66044443118978013452e-01, 5.97158591702786178956e-01, 3.96079766039156899726e-01, 1.73648177666930414453e-01, -5.81448289104757737311e-02, -2.86803232711090205775e-01, -4.99999999999999777955e-01, -6.86241637868733489469e-01, -8.35487811412936265398e-01, -9.39692620785908316883e-01, -9.93238357741943023171e-01, -9.93238357741943023171e-01, -9.39692620785908538927e-01, -8.35487811412936487443e-01, -6.86241637868733600492e-01, -5.00000000000000444089e-01, -2.86803232711090649865e-01, -5.81448289104762386370e-02, 1.73648177666930830787e-01, 3.96079766039156511148e-01, 5.97158591702785845889e-01, 7.66044443118977791407e-01, 8.93632640323412164030e-01, 9.73044870579824028312e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[27] = {0.00000000000000000000e+00f, 2.30615870742440165486e-01f, 4.48799180200462166646e-01f, 6.42787609686539251896e-01f, 8.02123192755043734614e-01f, 9.18216106880273996715e-01f, 9.84807753012208020316e-01f, 9.98308158271268175632e-01f, 9.57989512315488900285e-01f, 8.66025403784438707611e-01f, 7.27373641573048845821e-01f, 5.49508978070806231031e-01f, 3.42020143325668879442e-01f, 1.16092914125229929034e-01f, -1.16092914125230123323e-01f, -3.42020143325668213308e-01f, -5.49508978070806008986e-01f, -7.27373641573048623776e-01f, -8.66025403784438374544e-01f, -9.57989512315488789262e-01f, -9.98308158271268175632e-01f, -9.84807753012208020316e-01f, -9.18216106880274107738e-01f, -8.02123192755043956659e-01f, -6.42787609686539584963e-01f, -4.48799180200462444201e-01f, -2.30615870742439582619e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[27] = {0.00000000000000000000e+00, 2.30615870742440165486e-01, 4.48799180200462166646e-01, 6.42787609686539251896e-01, 8.02123192755043734614e-01, 9.18216106880273996715e-01, 9.84807753012208020316e-01, 9.98308158271268175632e-01, 9.57989512315488900285e-01, 8.66025403784438707611e-01, 7.27373641573048845821e-01, 5.49508978070806231031e-01, 3.42020143325668879442e-01, 1.16092914125229929034e-01, -1.16092914125230123323e-01, -3.42020143325668213308e-01, -5.49508978070806008986e-01, -7.27373641573048623776e-01, -8.66025403784438374544e-01, -9.57989512315488789262e-01, -9.98308158271268175632e-01, -9.84807753012208020316e-01, -9.18216106880274107738e-01, -8.02123192755043956659e-01, -6.42787609686539584963e-01, -4.48799180200462444201e-01, -2.30615870742439582619e-01};
     return v[m];
   }
 };
 template <> struct Roots<32> {
-  static __device__ __forceinline__ float c(int m) {
-    constexpr float v[32] = {1.00000000000000000000e+00f, 9.80785280403230430579e-01f, 9.23879532511286738483e-01f, 8.31469612302545235671e-01f, 7.07106781186547572737e-01f, 5.55570233019602288671e-01f, 3.82683432365089837290e-01f, 1.95090322016128331351e-01f, 0.00000000000000000000e+00f, -1.95090322016128192573e-01f, -3.82683432365089726268e-01f, -5.55570233019601955604e-01f, -7.07106781186547461715e-01f, -8.31469612302545346694e-01f, -9.23879532511286738483e-01f, -9.80785280403230430579e-01f, -1.00000000000000000000e+00f, -9.80785280403230430579e-01f, -9.23879532511286849505e-01f, -8.31469612302545457716e-01f, -7.07106781186547683760e-01f, -5.55570233019602177649e-01f, -3.82683432365090336891e-01f, -1.95090322016128664417e-01f, 0.00000000000000000000e+00f, 1.95090322016128303595e-01f, 3.82683432365090003824e-01f, 5.55570233019601844582e-01f, 7.07106781186547350693e-01f, 8.31469612302545235671e-01f, 9.23879532511286516439e-01f, 9.80785280403230319557e-01f};
+  static __device__ __forceinline__ rl c(int m) {
+    constexpr rl v[32] = {1.00000000000000000000e+00, 9.80785280403230430579e-01, 9.23879532511286738483e-01, 8.31469612302545235671e-01, 7.07106781186547572737e-01, 5.55570233019602288671e-01, 3.82683432365089837290e-01, 1.95090322016128331351e-01, 0.00000000000000000000e+00, -1.95090322016128192573e-01, -3.82683432365089726268e-01, -5.55570233019601955604e-01, -7.07106781186547461715e-01, -8.31469612302545346694e-01, -9.23879532511286738483e-01, -9.80785280403230430579e-01, -1.00000000000000000000e+00, -9.80785280403230430579e-01, -9.23879532511286849505e-01, -8.31469612302545457716e-01, -7.07106781186547683760e-01, -5.55570233019602177649e-01, -3.82683432365090336891e-01, -1.95090322016128664417e-01, 0.00000000000000000000e+00, 1.95090322016128303595e-01, 3.82683432365090003824e-01, 5.55570233019601844582e-01, 7.07106781186547350693e-01, 8.31469612302545235671e-01, 9.23879532511286516439e-01, 9.80785280403230319557e-01};
     return v[m];
   }
-  static __device__ __forceinline__ float s(int m) {
-    constexpr float v[32] = {0.00000000000000000000e+00f, 1.95090322016128248084e-01f, 3.82683432365089781779e-01f, 5.55570233019602177649e-01f, 7.07106781186547461715e-01f, 8.31469612302545235671e-01f, 9.23879532511286738483e-01f, 9.80785280403230430579e-01f, 1.00000000000000000000e+00f, 9.80785280403230430579e-01f, 9.23879532511286738483e-01f, 8.31469612302545457716e-01f, 7.07106781186547572737e-01f, 5.55570233019602177649e-01f, 3.82683432365089892802e-01f, 1.95090322016128608906e-01f, 0.00000000000000000000e+00f, -1.95090322016128359106e-01f, -3.82683432365089670757e-01f, -5.55570233019601955604e-01f, -7.07106781186547461715e-01f, -8.31469612302545235671e-01f, -9.23879532511286516439e-01f, -9.80785280403230319557e-01f, -1.00000000000000000000e+00f, -9.80785280403230430579e-01f, -9.23879532511286627461e-01f, -8.31469612302545457716e-01f, -7.07106781186547683760e-01f, -5.55570233019602177649e-01f, -3.82683432365090392402e-01f, -1.95090322016128719929e-01f};
+  static __device__ __forceinline__ rl s(int m) {
+    constexpr rl v[32] = {0.00000000000000000000e+00, 1.95090322016128248084e-01, 3.82683432365089781779e-01, 5.55570233019602177649e-01, 7.07106781186547461715e-01, 8.31469612302545235671e-01, 9.23879532511286738483e-01, 9.80785280403230430579e-01, 1.00000000000000000000e+00, 9.80785280403230430579e-01, 9.23879532511286738483e-01, 8.31469612302545457716e-01, 7.07106781186547572737e-01, 5.55570233019602177649e-01, 3.82683432365089892802e-01, 1.95090322016128608906e-01, 0.00000000000000000000e+00, -1.95090322016128359106e-01, -3.82683432365089670757e-01, -5.55570233019601955604e-01, -7.07106781186547461715e-01, -8.31469612302545235671e-01, -9.23879532511286516439e-01, -9.80785280403230319557e-01, -1.00000000000000000000e+00, -9.80785280403230430579e-01, -9.23879532511286627461e-01, -8.31469612302545457716e-01, -7.07106781186547683760e-01, -5.55570233019602177649e-01, -3.82683432365090392402e-01, -1.95090322016128719929e-01};
     return v[m];
   }
 };
 
 // multiply by exp(sign * 2 pi i m / R) for a compile-time m (after unrolling)
 template <int R>
-__device__ __forceinline__ float2 mul_root(float2 a, int m, float sign) {
+__device__ __forceinline__ cx mul_root(cx a, int m, rl sign) {
   m %= R;
   if (m == 0) return a;
   if (4 * m == R) return mul_si(a, sign);
-  if (2 * m == R) return make_float2(-a.x, -a.y);
+  if (2 * m == R) return make_cx(-a.x, -a.y);
   if (4 * m == 3 * R) return mul_si(a, -sign);
-  return cmul(a, make_float2(Roots<R>::c(m), sign * Roots<R>::s(m)));
+  return cmul(a, make_cx(Roots<R>::c(m), sign * Roots<R>::s(m)));
 }
 
 // Composite radix R = A*B (Cooley-Tukey inside the butterfly): DFT_A over j1
 // of u[B j1 + j2], twiddle W_R^(j2 k1), DFT_B over j2; output k1 + A k2.
 template <int A, int B>
 struct DftComposite {
-  static __device__ __forceinline__ void run(float2* u, float sign, const float2* tab, int S, int n) {
+  static __device__ __forceinline__ void run(cx* u, rl sign, const cx* tab, int S, int n) {
     constexpr int R = A * B;
-    float2 v[R];
+    cx v[R];
 #pragma unroll
     for (int j2 = 0; j2 < B; ++j2) {
-      float2 t[A];
+      cx t[A];
 #pragma unroll
       for (int j1 = 0; j1 < A; ++j1) t[j1] = u[B * j1 + j2];
       Dft<A>::run(t, sign, tab, S, n);
@@ -554,7 +583,7 @@ struct DftComposite {
     }
 #pragma unroll
     for (int k1 = 0; k1 < A; ++k1) {
-      float2 t[B];
+      cx t[B];
 #pragma unroll
       for (int j2 = 0; j2 < B; ++j2) t[j2] = v[j2 * A + k1];
       Dft<B>::run(t, sign, tab, S, n);
@@ -572,3 +601,5 @@ template <> struct Dft<20> : DftComposite<4, 5> {};
 template <> struct Dft<25> : DftComposite<5, 5> {};
 template <> struct Dft<27> : DftComposite<3, 9> {};
 template <> struct Dft<32> : DftComposite<4, 8> {};
+
+}  // namespace AF_NS

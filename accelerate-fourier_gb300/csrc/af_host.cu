@@ -11,7 +11,7 @@
 #include <map>
 #include <mutex>
 
-namespace af {
+namespace AF_NS {
 
 typedef std::complex<double> cd;
 
@@ -117,7 +117,7 @@ TwTable PlanRes::table(i64 n) {
     t.p = arena + arena_used;
     arena_used += (size_t)t.len;
   } else {
-    t.p = (float2*)dalloc(sizeof(float2) * t.len);
+    t.p = (cx*)dalloc(sizeof(cx) * t.len);
   }
   if (!dry) {
     cuda_check(launch_twiddle_table(t.p, n, (int)S, t.H, stream), "twiddle table");
@@ -136,24 +136,24 @@ const i64* PlanRes::line_table(const std::vector<i64>& offs) {
   return p;
 }
 
-const float2* PlanRes::pair_table(i64 a, i64 b, int* off_b) {
+const cx* PlanRes::pair_table(i64 a, i64 b, int* off_b) {
   auto key = std::make_pair(a, b);
   TwTable ta = table(a), tb = table(b);
   *off_b = ta.len;
   auto it = pair_tables.find(key);
   if (it != pair_tables.end()) return it->second;
-  float2* p = (float2*)dalloc(sizeof(float2) * (ta.len + tb.len));
+  cx* p = (cx*)dalloc(sizeof(cx) * (ta.len + tb.len));
   if (!dry) {
-    cuda_check(cudaMemcpy(p, ta.p, sizeof(float2) * ta.len, cudaMemcpyDeviceToDevice), "table copy");
-    cuda_check(cudaMemcpy(p + ta.len, tb.p, sizeof(float2) * tb.len, cudaMemcpyDeviceToDevice), "table copy");
+    cuda_check(cudaMemcpy(p, ta.p, sizeof(cx) * ta.len, cudaMemcpyDeviceToDevice), "table copy");
+    cuda_check(cudaMemcpy(p + ta.len, tb.p, sizeof(cx) * tb.len, cudaMemcpyDeviceToDevice), "table copy");
   }
   pair_tables[key] = p;
   return p;
 }
 
-static std::vector<float2> to_f32(const std::vector<cd>& v) {
-  std::vector<float2> o(v.size());
-  for (size_t i = 0; i < v.size(); ++i) o[i] = make_float2((float)v[i].real(), (float)v[i].imag());
+static std::vector<cx> to_cx(const std::vector<cd>& v) {
+  std::vector<cx> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i) o[i] = make_cx((rl)v[i].real(), (rl)v[i].imag());
   return o;
 }
 
@@ -206,7 +206,7 @@ const RaderRes& PlanRes::rader_res(i64 p, int sign) {
   host_tabs[r.gpow] = gpow;
   if (dry) {
     r.M = M;
-    r.zs = (float2*)dalloc(sizeof(float2) * M);
+    r.zs = (cx*)dalloc(sizeof(cx) * M);
     rader[key] = r;
     return rader[key];
   }
@@ -231,10 +231,10 @@ const RaderRes& PlanRes::rader_res(i64 p, int sign) {
     for (i64 i = 1; i < m; ++i) kk[M - i] = kern[m - i];
   fft64(kk.data(), 1, S.data(), M, +1);
   for (auto& v : S) v /= (double)M;
-  std::vector<float2> zs = to_f32(S);
-  r.zs = (float2*)dalloc(sizeof(float2) * M);
+  std::vector<cx> zs = to_cx(S);
+  r.zs = (cx*)dalloc(sizeof(cx) * M);
   r.M = M;
-  cuda_check(cudaMemcpy(r.zs, zs.data(), sizeof(float2) * M, cudaMemcpyHostToDevice), "rader spectrum");
+  cuda_check(cudaMemcpy(r.zs, zs.data(), sizeof(cx) * M, cudaMemcpyHostToDevice), "rader spectrum");
   rader[key] = r;
   return rader[key];
 }
@@ -249,8 +249,8 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
   c.len = len;
   c.pad = pad;
   if (dry) {
-    c.chirp = (float2*)dalloc(sizeof(float2) * len);
-    c.spec = (float2*)dalloc(sizeof(float2) * pad);
+    c.chirp = (cx*)dalloc(sizeof(cx) * len);
+    c.spec = (cx*)dalloc(sizeof(cx) * pad);
     chirps[key] = c;
     return chirps[key];
   }
@@ -265,19 +265,19 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
   fft64(cj.data(), 1, spec.data(), pad, +1);
   for (auto& v : spec) v /= (double)pad;
   std::vector<cd> head(ch.begin(), ch.begin() + len);
-  std::vector<float2> hf = to_f32(head), sf = to_f32(spec);
-  c.chirp = (float2*)dalloc(sizeof(float2) * len);
-  c.spec = (float2*)dalloc(sizeof(float2) * pad);
-  cuda_check(cudaMemcpy(c.chirp, hf.data(), sizeof(float2) * len, cudaMemcpyHostToDevice), "chirp");
-  cuda_check(cudaMemcpy(c.spec, sf.data(), sizeof(float2) * pad, cudaMemcpyHostToDevice), "chirp");
+  std::vector<cx> hf = to_cx(head), sf = to_cx(spec);
+  c.chirp = (cx*)dalloc(sizeof(cx) * len);
+  c.spec = (cx*)dalloc(sizeof(cx) * pad);
+  cuda_check(cudaMemcpy(c.chirp, hf.data(), sizeof(cx) * len, cudaMemcpyHostToDevice), "chirp");
+  cuda_check(cudaMemcpy(c.spec, sf.data(), sizeof(cx) * pad, cudaMemcpyHostToDevice), "chirp");
   chirps[key] = c;
   return chirps[key];
 }
 
 
 // ============================================================ tile building
-// elements per CTA the ping-pong tile can hold (two padded buffers + tables)
-static const i64 kTileCap = 13000;
+// longest line one tile holds (two ping-pong buffers in 227 KB of shared memory)
+static const i64 kTileCap = sizeof(cx) == 8 ? 13000 : 6200;
 
 // Radix sequence of a tile phase: the fewest Stockham passes over the
 // supported butterflies (prime radices 2..13 and the composites built from
@@ -341,7 +341,7 @@ static bool four_step_split(i64 n, i64* n1, i64* n2) {
   return true;
 }
 
-static void fill_phase(FftPhase& ph, i64 n, float sign, int ls, int es, int lcnt, int tw_off, int S_log2) {
+static void fill_phase(FftPhase& ph, i64 n, rl sign, int ls, int es, int lcnt, int tw_off, int S_log2) {
   memset(&ph, 0, sizeof ph);
   ph.n = (int)n;
   ph.ls = ls;
@@ -392,8 +392,9 @@ static const int kMaxTw = 512;
 static const int kMaxG = 128;
 static void choose_geometry(i64 slen, i64 lines, int tw_total, bool want_wide, int* threads, int* G) {
   if (tw_total > kMaxTw) throw AfError(AF_ERR_UNSUPPORTED, "twiddle tables exceed the tile allowance");
-  const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - 8 * kMaxTw - 32 * kMaxG - 256;
-  auto fits = [&](i64 g) { return 2 * 8 * (spad_host((int)(g * slen)) + 2) <= budget; };
+  const i64 es = (i64)sizeof(cx);
+  const i64 budget = 227 * 1024 - (i64)((sizeof(TileDesc) + 15) / 16 * 16) - es * kMaxTw - 4 * es * kMaxG - 256;
+  auto fits = [&](i64 g) { return 2 * es * (spad_host((int)(g * slen)) + 2) <= budget; };
   // about 4096 elements per CTA keeps three CTAs resident per SM; strided
   // (line-fast) tiles take at least 4 lines, one 32-byte sector per row
   i64 g = std::max<i64>(1, 4096 / std::max<i64>(slen, 1));
@@ -416,7 +417,8 @@ struct TileStep {
 };
 
 // Wavefronts of one half-warp's 64-bit shared accesses: the busiest of the
-// 16 float2 banks serves one wavefront per distinct address.
+// 16 eight-byte bank pairs serves one wavefront per distinct address (the
+// model of FP32 elements; FP64 tiles use the same choice).
 static int half_warp_wavefronts(int* a, int cnt) {
   std::sort(a, a + cnt);
   int per_bank[16] = {0}, worst = 0;
@@ -519,7 +521,7 @@ static TileDesc blank_desc() {
 }
 
 // plain tile: FFT of length n (sign) over `lines` lines, optional store twiddle W_ptwN^(lo e)
-static TileStep plain_step(PlanRes& res, i64 n, float sign, i64 lines, const View& in, const View& out,
+static TileStep plain_step(PlanRes& res, i64 n, rl sign, i64 lines, const View& in, const View& out,
                            i64 ptwN = 0) {
   TileStep s;
   s.d = blank_desc();
@@ -574,7 +576,7 @@ static bool single_tile_ok(const Node* nd) {
 }
 
 // Good-Thomas tile (Planned.hs:584-617): grid m x n, n = first factor
-static TileStep gt_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+static TileStep gt_step(PlanRes& res, const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
   const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
   TileStep s;
   s.d = blank_desc();
@@ -604,7 +606,7 @@ static TileStep gt_step(PlanRes& res, const Node* nd, float sign, i64 lines, con
 }
 
 // Rader tile (Planned.hs:646-692), convolution length M = rader_conv_len(p)
-static TileStep rader_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+static TileStep rader_step(PlanRes& res, const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
   const i64 p = nd->n;
   const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
   const i64 M = rr.M;
@@ -632,7 +634,7 @@ static TileStep rader_step(PlanRes& res, const Node* nd, float sign, i64 lines, 
 }
 
 // Bluestein tile (Planned.hs:760-773)
-static TileStep chirp_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+static TileStep chirp_step(PlanRes& res, const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
   const i64 N = nd->n, M = nd->a->n;
   const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
   TileStep s;
@@ -658,7 +660,7 @@ static TileStep chirp_step(PlanRes& res, const Node* nd, float sign, i64 lines, 
   return s;
 }
 
-static TileStep single_step(PlanRes& res, const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+static TileStep single_step(PlanRes& res, const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
   if (gt_tile_ok(nd)) return gt_step(res, nd, sign, lines, in, out);
   if (rader_tile_ok(nd)) return rader_step(res, nd, sign, lines, in, out);
   if (chirp_tile_ok(nd)) return chirp_step(res, nd, sign, lines, in, out);
@@ -681,7 +683,7 @@ struct MultiPass {
 // split-radix chain of Planned.hs:490-522 for even sizes): pass A FFT_n1 over
 // columns x[n2 j1 + j2] with twiddle W_n^(j2 k1), pass B FFT_n2 over rows,
 // X[k1 + n1 k2].
-static bool four_step_plan(PlanRes& res, i64 n, float sign, i64 T, i64 wst, const View& inb,
+static bool four_step_plan(PlanRes& res, i64 n, rl sign, i64 T, i64 wst, const View& inb,
                            const View& outb, i64 ws_base, MultiPass* mp) {
   i64 n1, n2;
   if (!four_step_split(n, &n1, &n2)) return false;
@@ -705,7 +707,7 @@ static bool four_step_plan(PlanRes& res, i64 n, float sign, i64 T, i64 wst, cons
 // and stores transposed; pass 2 transforms the second factor m over rows and
 // scatters by the CRT map r = CRT(q, p).  Either factor may be any
 // single-tile transform (split-radix, Rader, Bluestein, Good-Thomas tile).
-static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+static bool gt_two_pass_plan(PlanRes& res, const Node* nd, rl sign, i64 T, i64 wst, const View& inb,
                              const View& outb, i64 ws_base, MultiPass* mp) {
   const Node* na = nd->a;
   const Node* nb = nd->b;
@@ -746,7 +748,7 @@ static bool gt_two_pass_plan(PlanRes& res, const Node* nd, float sign, i64 T, i6
 //   R   rows:    FFT_n2(+1), * S[k1 + n1 k2], FFT_n2(-1), twiddle W_M^(-j2 k1)
 //   A'  columns: FFT_n1(-1) over k1 -> c[n2 j1 + j2]
 // The load of A and the store of A' carry the Rader or Bluestein maps.
-static bool conv_plan(PlanRes& res, i64 M, const float2* S, i64 T, i64 wst, const View& inb,
+static bool conv_plan(PlanRes& res, i64 M, const cx* S, i64 T, i64 wst, const View& inb,
                       const View& outb, i64 ws_base, MultiPass* mp, TileStep** a_step, TileStep** o_step,
                       i64 dc_off) {
   i64 n1, n2;
@@ -785,7 +787,7 @@ static bool conv_plan(PlanRes& res, i64 M, const float2* S, i64 T, i64 wst, cons
 
 // Rader in three passes: the conv of length M with the dlog gather/scatter
 // fused into the first load and the last store (x0 and DC fix-up included).
-static bool rader_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+static bool rader_conv_plan(PlanRes& res, const Node* nd, rl sign, i64 T, i64 wst, const View& inb,
                             const View& outb, i64 ws_base, MultiPass* mp) {
   const i64 p = nd->n;
   const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
@@ -822,7 +824,7 @@ static bool rader_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64
 
 // Bluestein in three passes: chirp * x (zero padded) fused into the first
 // load, chirp * take N into the last store.
-static bool chirp_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+static bool chirp_conv_plan(PlanRes& res, const Node* nd, rl sign, i64 T, i64 wst, const View& inb,
                             const View& outb, i64 ws_base, MultiPass* mp) {
   const i64 N = nd->n, M = nd->a->n;
   const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
@@ -845,7 +847,7 @@ static bool chirp_conv_plan(PlanRes& res, const Node* nd, float sign, i64 T, i64
   return true;
 }
 
-static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+static bool multi_pass(PlanRes& res, const Node* nd, rl sign, i64 T, i64 wst, const View& inb,
                        const View& outb, i64 ws_base, MultiPass* mp);
 
 // workspace stride of a transform's multi-pass scheme
@@ -860,7 +862,7 @@ static i64 multi_pass_len(const Node* nd) {
 // composite's first factor) runs as strided columns with the twiddle, and the
 // remaining node (Good-Thomas, Rader, Bluestein, ...) runs over the rows
 // with its own single-tile or multi-pass scheme, storing X[k1 + n1 k2].
-static bool peel_plan(PlanRes& res, const Node* nd, float sign, i64 T, const View& inb, const View& outb,
+static bool peel_plan(PlanRes& res, const Node* nd, rl sign, i64 T, const View& inb, const View& outb,
                       i64 ws_base, MultiPass* mp) {
   if (T != 1) return false;
   const i64 n = nd->n;
@@ -917,7 +919,7 @@ static bool peel_plan(PlanRes& res, const Node* nd, float sign, i64 T, const Vie
 // two-pass Good-Thomas, primes as three-pass Rader, chirp nodes as
 // three-pass Bluestein, other split-radix/composite nodes by peeling.
 // inb/outb: single-level views whose s_hi is the stride between transforms.
-static bool multi_pass(PlanRes& res, const Node* nd, float sign, i64 T, i64 wst, const View& inb,
+static bool multi_pass(PlanRes& res, const Node* nd, rl sign, i64 T, i64 wst, const View& inb,
                        const View& outb, i64 ws_base, MultiPass* mp) {
   mp->steps.clear();
   switch (nd->kind) {
@@ -1045,17 +1047,17 @@ void finalize_program(PlanRes& res, Program& prog) {
   cuda_check(cudaMemcpy(prog.dblob, host.data(), bytes, cudaMemcpyHostToDevice), "program upload");
 }
 
-TileBases make_bases(const float* in_re, const float* in_im, float* out_re, float* out_im, float2* ws,
-                     const float* aux_re, const float* aux_im) {
+TileBases make_bases(const rl* in_re, const rl* in_im, rl* out_re, rl* out_im, cx* ws,
+                     const rl* aux_re, const rl* aux_im) {
   TileBases b;
   memset(&b, 0, sizeof b);
-  if (in_im) { b.re[BUF_IN] = (float*)in_re; b.im[BUF_IN] = (float*)in_im; }
-  else b.c[BUF_IN] = (float2*)in_re;
+  if (in_im) { b.re[BUF_IN] = (rl*)in_re; b.im[BUF_IN] = (rl*)in_im; }
+  else b.c[BUF_IN] = (cx*)in_re;
   if (out_im) { b.re[BUF_OUT] = out_re; b.im[BUF_OUT] = out_im; }
-  else b.c[BUF_OUT] = (float2*)out_re;
+  else b.c[BUF_OUT] = (cx*)out_re;
   b.c[BUF_WS] = ws;
-  if (aux_im) { b.re[BUF_AUX] = (float*)aux_re; b.im[BUF_AUX] = (float*)aux_im; }
-  else b.c[BUF_AUX] = (float2*)aux_re;
+  if (aux_im) { b.re[BUF_AUX] = (rl*)aux_re; b.im[BUF_AUX] = (rl*)aux_im; }
+  else b.c[BUF_AUX] = (cx*)aux_re;
   return b;
 }
 
@@ -1149,7 +1151,7 @@ struct Lowering {
   }
 
   // Transform `lines` rows through any 2-level views.
-  void node(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  void node(const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
     const i64 n = nd->n;
     if (n == 0 || lines == 0) return;
     if (n == 1) {
@@ -1202,7 +1204,7 @@ struct Lowering {
   // Cooley-Tukey four-step with a recursive row transform (sizes whose rows
   // do not fit one tile): columns n1 = power of two from the SR chain or the
   // composite's first factor.
-  void recursive_four_step(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  void recursive_four_step(const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
     const i64 n = nd->n;
     i64 n1;
     const Node* sub2;
@@ -1255,7 +1257,7 @@ struct Lowering {
   }
 
   // Good-Thomas through explicit CRT maps (Planned.hs:584-617)
-  void good_thomas(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  void good_thomas(const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
     const i64 n = nd->a->n, m = nd->b->n, N = nd->n;
     const i64 mark = top;
     const i64 W1 = alloc(lines * N), W2 = alloc(lines * N);
@@ -1278,7 +1280,7 @@ struct Lowering {
 
   // Rader through explicit permutation maps and the sub-plan of p-1
   // (Planned.hs:646-692); used only when p-1 has no fused scheme
-  void rader_multi(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  void rader_multi(const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
     const i64 p = nd->n, m = p - 1;
     const RaderRes& rr = res.rader_res(p, sign > 0 ? 1 : -1);
     if (rr.M != m) throw AfError(AF_ERR_UNSUPPORTED, "Rader length without a fused scheme");
@@ -1304,7 +1306,7 @@ struct Lowering {
   }
 
   // Bluestein through explicit chirp maps (Planned.hs:760-773)
-  void bluestein_multi(const Node* nd, float sign, i64 lines, const View& in, const View& out) {
+  void bluestein_multi(const Node* nd, rl sign, i64 lines, const View& in, const View& out) {
     const i64 N = nd->n, M = nd->a->n;
     const ChirpRes& cr = res.chirp_res(N, M, sign > 0 ? 1 : -1);
     const i64 mark = top;
@@ -1326,7 +1328,7 @@ struct Lowering {
   }
 };
 
-void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Program* prog) {
+void build_program(PlanRes& res, const Node* root, rl sign, i64 batch, Program* prog) {
   Lowering L{res, prog};
   prog->launches.clear();
   View in = View::rows(BUF_IN, 0, root->n, batch);
@@ -1336,7 +1338,7 @@ void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Progra
   finalize_program(res, *prog);
 }
 
-void build_program_view(PlanRes& res, const Node* root, float sign, i64 lines, const View& in, const View& out,
+void build_program_view(PlanRes& res, const Node* root, rl sign, i64 lines, const View& in, const View& out,
                         Program* prog) {
   Lowering L{res, prog};
   prog->launches.clear();
@@ -1359,7 +1361,7 @@ struct BatchPlan {
   PlanRes res;
   Program fwd, inv, cot;  // sign, -sign, sign with the cotangent epilogue
   i64 ws_elems = 0;
-  float2* ws = nullptr;
+  cx* ws = nullptr;
   i64 fallback = 0;      // transforms executed through their own programs
   bool cot_ok = true;    // every transform has a fused program for the cotangent epilogue
   i64 bluestein_fallbacks = 0;  // transforms whose tree has no fused scheme (run as chirp-z)
@@ -1369,7 +1371,7 @@ struct BatchPlan {
 static const i64 kChunkElems = (i64)3 << 20;  // 24 MB of workspace per L2 chunk
 static const int kLanes = 3;                   // chunks in flight (72 MB of workspace in L2)
 
-static void build_batch_program(BatchPlan* B, float sign, Program& prog,
+static void build_batch_program(BatchPlan* B, rl sign, Program& prog,
                                 std::vector<std::pair<i64, Program>>& fallback, bool cot) {
   prog.launches.clear();
   fallback.clear();
@@ -1584,10 +1586,10 @@ BatchPlan* batch_create_mode(const i64* ns, i64 count, int sign, bool dry) {
       o += ns[i];
     }
     if (o >= ((i64)1 << 31)) throw AfError(AF_ERR_UNSUPPORTED, "total length must be below 2^31");
-    build_batch_program(B, (float)sign, B->fwd, B->fb_fwd, false);
-    build_batch_program(B, (float)-sign, B->inv, B->fb_inv, false);
+    build_batch_program(B, (rl)sign, B->fwd, B->fb_fwd, false);
+    build_batch_program(B, (rl)-sign, B->inv, B->fb_inv, false);
     std::vector<std::pair<i64, Program>> fb_cot;
-    build_batch_program(B, (float)sign, B->cot, fb_cot, true);
+    build_batch_program(B, (rl)sign, B->cot, fb_cot, true);
     B->cot_ok = fb_cot.empty();
     i64 ws = std::max(std::max(B->fwd.ws_elems, B->inv.ws_elems), B->cot.ws_elems);
     for (auto& f : B->fb_fwd) ws = std::max(ws, f.second.ws_elems);
@@ -1595,7 +1597,7 @@ BatchPlan* batch_create_mode(const i64* ns, i64 count, int sign, bool dry) {
     B->fallback = (i64)B->fb_fwd.size();
     B->ws_elems = ws;
     if (!dry) {
-      if (ws) cuda_check(cudaMalloc(&B->ws, sizeof(float2) * ws), "batch workspace");
+      if (ws) cuda_check(cudaMalloc(&B->ws, sizeof(cx) * ws), "batch workspace");
       cuda_check(cudaDeviceSynchronize(), "batch tables");
     }
   } catch (...) {
@@ -1612,24 +1614,24 @@ void batch_destroy(BatchPlan* B) {
   delete B;
 }
 
-cudaError_t batch_run(BatchPlan* B, bool inverse, const float2* in, float2* out, const float* w, double* loss,
+cudaError_t batch_run(BatchPlan* B, bool inverse, const cx* in, cx* out, const rl* w, double* loss,
                       cudaStream_t st) {
   if (w && !B->cot_ok) throw AfError(AF_ERR_UNSUPPORTED, "cotangent epilogue needs fused programs for every length");
   const Program& prog = w ? B->cot : (inverse ? B->inv : B->fwd);
-  TileBases bases = make_bases((const float*)in, nullptr, (float*)out, nullptr, B->ws, w, nullptr);
+  TileBases bases = make_bases((const rl*)in, nullptr, (rl*)out, nullptr, B->ws, w, nullptr);
   if (w) {
-    // weights are real: BUF_AUX is read as a float plane indexed like the output
+    // weights are real: BUF_AUX is read as a rl plane indexed like the output
     bases.c[BUF_AUX] = nullptr;
-    bases.re[BUF_AUX] = (float*)w;
+    bases.re[BUF_AUX] = (rl*)w;
   }
   cudaError_t e = run_program(prog, bases, loss, st);
   if (e != cudaSuccess) return e;
   if (w) return cudaSuccess;
   for (auto& f : (inverse ? B->fb_inv : B->fb_fwd)) {
     const i64 o = B->offs[f.first];
-    TileBases b2 = make_bases((const float*)(in + o), nullptr, (float*)(out + o), nullptr, B->ws,
+    TileBases b2 = make_bases((const rl*)(in + o), nullptr, (rl*)(out + o), nullptr, B->ws,
                               w ? w + o : nullptr, nullptr);
-    if (w) { b2.c[BUF_AUX] = nullptr; b2.re[BUF_AUX] = (float*)(w + o); }
+    if (w) { b2.c[BUF_AUX] = nullptr; b2.re[BUF_AUX] = (rl*)(w + o); }
     e = run_program(f.second, b2, loss, st);
     if (e != cudaSuccess) return e;
   }

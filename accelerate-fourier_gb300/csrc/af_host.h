@@ -10,13 +10,21 @@
 #include "../../include/af.h"
 #include "af_internal.h"
 #include "af_plan.h"
+#include "af_f64.h"
 
+// Shared by both precisions of the engine.
 namespace af {
 
 struct AfError : std::runtime_error {
   af_status code;
   AfError(af_status c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
+void set_last_error(const std::string& m);
+const Node* plan_root(Planner& pl, i64 n, int algo);
+
+}  // namespace af
+
+namespace AF_NS {
 
 // A batch of lines: line l = hi * lo_cnt + lo, element e at
 // off + hi*s_hi + lo*s_lo + e*s_e in buffer `buf` (complex units).
@@ -68,7 +76,7 @@ struct Program {
 };
 
 struct TwTable {
-  float2* p = nullptr;
+  cx* p = nullptr;
   int S_log2 = 0, H = 0, len = 0;
 };
 
@@ -78,21 +86,21 @@ struct RaderRes {
   int* src = nullptr;    // src[q] = 1 + perm[(-q) mod (p-1)] = g^-q mod p
   int* inv = nullptr;    // inverse permutation
   int* gpow = nullptr;   // gpow[q] = g^q mod p (scatter target of conv index q)
-  float2* zs = nullptr;  // kernel spectrum / M (M entries)
+  cx* zs = nullptr;  // kernel spectrum / M (M entries)
   i64 M = 0;             // conv transform length (rader_conv_len)
 };
 i64 rader_conv_len(i64 p);
 
 struct ChirpRes {
   i64 len = 0, pad = 0;
-  float2* chirp = nullptr;  // len entries
-  float2* spec = nullptr;   // pad entries
+  cx* chirp = nullptr;  // len entries
+  cx* spec = nullptr;   // pad entries
 };
 
 struct PlanRes {
   bool dry = false;                       // address-checking mode (no device)
   bool no_alloc = false;                  // any device allocation is an error
-  float2* arena = nullptr;                // when set, twiddle tables come from this
+  cx* arena = nullptr;                // when set, twiddle tables come from this
   size_t arena_cap = 0, arena_used = 0;   // preallocated device area (no allocation)
   char* blob = nullptr;                   // when set, programs upload here
   size_t blob_cap = 0;
@@ -102,14 +110,14 @@ struct PlanRes {
   std::map<const void*, std::vector<i64>> host_loffs; // host copies of gathered-line tables
   std::vector<void*> allocs;
   std::map<i64, TwTable> tables;
-  std::map<std::pair<i64, i64>, const float2*> pair_tables;
+  std::map<std::pair<i64, i64>, const cx*> pair_tables;
   std::map<std::pair<i64, int>, RaderRes> rader;
   std::map<std::tuple<i64, i64, int>, ChirpRes> chirps;
   std::vector<cudaStream_t> streams;  // owned side streams of programs
   std::vector<cudaEvent_t> events;
   void* dalloc(size_t bytes);
   TwTable table(i64 n);
-  const float2* pair_table(i64 a, i64 b, int* off_b);
+  const cx* pair_table(i64 a, i64 b, int* off_b);
   const RaderRes& rader_res(i64 p, int sign);
   const ChirpRes& chirp_res(i64 len, i64 pad, int sign);
   const i64* line_table(const std::vector<i64>& offs);  // device copy of line offsets
@@ -117,16 +125,15 @@ struct PlanRes {
 };
 
 bool tile_ok(i64 n);
-void set_last_error(const std::string& m);
 void finalize_program(PlanRes& res, Program& prog);
 cudaError_t run_program(const Program& prog, const TileBases& bases, double* loss, cudaStream_t st);
-TileBases make_bases(const float* in_re, const float* in_im, float* out_re, float* out_im, float2* ws,
-                     const float* aux_re, const float* aux_im);
+TileBases make_bases(const rl* in_re, const rl* in_im, rl* out_re, rl* out_im, cx* ws,
+                     const rl* aux_re, const rl* aux_im);
 
 // Builds the launch program of one plan tree over `batch` contiguous rows.
-void build_program(PlanRes& res, const Node* root, float sign, i64 batch, Program* prog);
+void build_program(PlanRes& res, const Node* root, rl sign, i64 batch, Program* prog);
 // The same over `lines` lines addressed through two-level views (strided axes).
-void build_program_view(PlanRes& res, const Node* root, float sign, i64 lines, const View& in, const View& out,
+void build_program_view(PlanRes& res, const Node* root, rl sign, i64 lines, const View& in, const View& out,
                         Program* prog);
 
 // Batched executor: many transforms of mixed lengths, concatenated.
@@ -135,10 +142,10 @@ BatchPlan* batch_create(const i64* ns, i64 count, int sign);
 BatchPlan* batch_create_mode(const i64* ns, i64 count, int sign, bool dry);
 void batch_destroy(BatchPlan* b);
 const void* batch_res(BatchPlan* B);
-const Node* plan_root(Planner& pl, i64 n, int algo);
 
 }  // namespace af
 
+#ifndef AF_F64
 struct af_plan_s {
   long long n = 0;
   int sign = -1;
@@ -152,5 +159,7 @@ struct af_plan_s {
   size_t ws_elems = 0;
   float2* stage = nullptr;  // staging for the real transforms and convolutions
   size_t stage_elems = 0;
+  af64::Plan* p64 = nullptr;  // set for a Complex Double plan (af_plan_create_f64)
   ~af_plan_s();
 };
+#endif

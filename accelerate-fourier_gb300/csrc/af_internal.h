@@ -4,7 +4,7 @@
 #include <stdint.h>
 #include "af_device.cuh"
 
-namespace af {
+namespace AF_NS {
 
 __host__ __device__ __forceinline__ int spad_host(int i, int sh = 4) { return i + (i >> sh); }
 
@@ -15,7 +15,7 @@ struct LaunchSpec {
   const WorkItem* items;
   int nitems;
   int threads;
-  int smem_data;      // float2 per ping-pong buffer (max over the launch's descriptors)
+  int smem_data;      // cx per ping-pong buffer (max over the launch's descriptors)
   int generic;        // 0: every descriptor is a one-phase PLAIN tile with AFFINE views
   size_t smem_bytes;  // dynamic shared memory of the launch
 };
@@ -44,19 +44,20 @@ struct MapDesc {
   IoDesc in, out;
   i64 n, m, nm;        // map parameters
   const int* tab;
-  const float2* vec;
+  const cx* vec;
   i64 dc_ws, x0_ws;    // workspace offsets of the per-line DC / x0 (-1 = none)
-  const float2* tab_tw;  // two-level twiddle table of n (MAP_TWIDDLE)
+  const cx* tab_tw;  // two-level twiddle table of n (MAP_TWIDDLE)
   int tw_log2;
-  float tw_sign;
-  float scale;
+  rl tw_sign;
+  rl scale;
 };
 cudaError_t launch_map(const MapDesc& d, const TileBases& bases, cudaStream_t st);
 
 // ------------------------------------------------------------- tables (FP64)
 // tab[i] = exp(-2 pi i t_i / n) for the two-level layout: t_i = i (i < S),
-// t_i = (i - S) * S (S <= i < S + H); computed in double, rounded to float.
-cudaError_t launch_twiddle_table(float2* dst, i64 n, int S, int H, cudaStream_t st);
+// t_i = (i - S) * S (S <= i < S + H); computed in double, rounded to the
+// element type.
+cudaError_t launch_twiddle_table(cx* dst, i64 n, int S, int H, cudaStream_t st);
 // chirp[k] = exp(sign * i * pi * sk^2 / len), sk = k for 2k < pad else k - pad,
 // with sk^2 reduced mod 2*len in exact integers (Private.hs:428-436).
 cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cudaStream_t st);
@@ -66,17 +67,17 @@ cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream
 // ------------------------------------------------------------- real / two-real / convolution maps
 // A complex array: interleaved when c is set, else planar re/im.
 struct CPtr {
-  float2* c;
-  float* re;
-  float* im;
+  cx* c;
+  rl* re;
+  rl* im;
 };
-cudaError_t launch_real_untangle(const float2* Z, CPtr out, i64 n2, i64 nout, i64 rows, const float2* tab,
+cudaError_t launch_real_untangle(const cx* Z, CPtr out, i64 n2, i64 nout, i64 rows, const cx* tab,
                                  int S_log2, cudaStream_t st);
-cudaError_t launch_real_entangle(CPtr spec, float2* f, i64 n2, i64 rows, const float2* tab, int S_log2, int herm,
+cudaError_t launch_real_entangle(CPtr spec, cx* f, i64 n2, i64 rows, const cx* tab, int S_log2, int herm,
                                  cudaStream_t st);
 cudaError_t launch_untangle(CPtr S, CPtr A, CPtr B, i64 h, i64 w, i64 total, cudaStream_t st);
 cudaError_t launch_reverse2d(CPtr in, CPtr out, i64 h, i64 w, i64 total, cudaStream_t st);
 cudaError_t launch_entangle(CPtr C, CPtr D, CPtr out, i64 total, cudaStream_t st);
-cudaError_t launch_conv_mul(float2* gx, const float2* gy, float s, i64 total, cudaStream_t st);
+cudaError_t launch_conv_mul(cx* gx, const cx* gy, rl s, i64 total, cudaStream_t st);
 
 }  // namespace af

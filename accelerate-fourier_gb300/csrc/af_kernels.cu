@@ -4,7 +4,7 @@
 // kernel tables.
 #include "af_internal.h"
 
-namespace af {
+namespace AF_NS {
 
 __device__ __forceinline__ i64 view_addr(const IoDesc& io, i64 line, i64 e) {
   const i64 lo_cnt = io.lo_div.d;
@@ -12,22 +12,22 @@ __device__ __forceinline__ i64 view_addr(const IoDesc& io, i64 line, i64 e) {
   const i64 lo = line - hi * lo_cnt;
   return io.off + hi * io.s_hi + lo * io.s_lo + e * io.s_e;
 }
-__device__ __forceinline__ float2 vload(const TileBases& B, const IoDesc& io, i64 a) {
+__device__ __forceinline__ cx vload(const TileBases& B, const IoDesc& io, i64 a) {
   if (B.c[io.buf]) return B.c[io.buf][a];
-  return make_float2(B.re[io.buf][a], B.im[io.buf][a]);
+  return make_cx(B.re[io.buf][a], B.im[io.buf][a]);
 }
-__device__ __forceinline__ void vstore(const TileBases& B, const IoDesc& io, i64 a, float2 v) {
+__device__ __forceinline__ void vstore(const TileBases& B, const IoDesc& io, i64 a, cx v) {
   if (B.c[io.buf]) B.c[io.buf][a] = v;
   else { B.re[io.buf][a] = v.x; B.im[io.buf][a] = v.y; }
 }
 
 __global__ void map_kernel(const MapDesc d, const TileBases B) {
   const i64 total = d.nlines * d.nout;
-  float2* ws = B.c[BUF_WS];
+  cx* ws = B.c[BUF_WS];
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
     const i64 line = q / d.nout;
     const i64 e = q - line * d.nout;
-    float2 v;
+    cx v;
     switch (d.mode) {
       case MAP_COPY: v = vload(B, d.in, view_addr(d.in, line, e)); break;
       case MAP_GT_IN: {
@@ -43,16 +43,16 @@ __global__ void map_kernel(const MapDesc d, const TileBases B) {
         if (d.x0_ws >= 0 && e == 0) ws[d.x0_ws + line] = vload(B, d.in, view_addr(d.in, line, 0));
         break;
       case MAP_RADER_OUT: {
-        const float2 x0 = ws[d.x0_ws + line];
-        const float2 c = e == 0 ? ws[d.dc_ws + line] : vload(B, d.in, view_addr(d.in, line, d.tab[e - 1]));
+        const cx x0 = ws[d.x0_ws + line];
+        const cx c = e == 0 ? ws[d.dc_ws + line] : vload(B, d.in, view_addr(d.in, line, d.tab[e - 1]));
         v = cadd(x0, c);
         break;
       }
       case MAP_CHIRP_IN:
-        v = e < d.n ? cmul(d.vec[e], vload(B, d.in, view_addr(d.in, line, e))) : make_float2(0.f, 0.f);
+        v = e < d.n ? cmul(d.vec[e], vload(B, d.in, view_addr(d.in, line, e))) : make_cx(0.f, 0.f);
         break;
       case MAP_MUL: {
-        const float2 u = vload(B, d.in, view_addr(d.in, line, e));
+        const cx u = vload(B, d.in, view_addr(d.in, line, e));
         if (d.dc_ws >= 0 && e == 0) ws[d.dc_ws + line] = u;
         v = cmul(d.vec[e], u);
         break;
@@ -61,9 +61,9 @@ __global__ void map_kernel(const MapDesc d, const TileBases B) {
       case MAP_TWIDDLE: {
         const i64 col = line % d.m;
         const i64 t = (col * e) % d.n;
-        const float2 lo = d.tab_tw[t & ((1 << d.tw_log2) - 1)];
-        const float2 hi = d.tab_tw[(1 << d.tw_log2) + (t >> d.tw_log2)];
-        float2 w = cmul(hi, lo);
+        const cx lo = d.tab_tw[t & ((1 << d.tw_log2) - 1)];
+        const cx hi = d.tab_tw[(1 << d.tw_log2) + (t >> d.tw_log2)];
+        cx w = cmul(hi, lo);
         w.y *= -d.tw_sign;
         v = cmul(vload(B, d.in, view_addr(d.in, line, e)), w);
         break;
@@ -88,16 +88,16 @@ cudaError_t launch_map(const MapDesc& d, const TileBases& bases, cudaStream_t st
 }
 
 // ------------------------------------------------------------- FP64 tables
-__global__ void twiddle_table_kernel(float2* dst, i64 n, int S, int H) {
+__global__ void twiddle_table_kernel(cx* dst, i64 n, int S, int H) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S + H) return;
   i64 t = i < S ? (i64)i : (i64)(i - S) * S;
   t %= n;
   double s, c;
   sincospi(2.0 * (double)t / (double)n, &s, &c);
-  dst[i] = make_float2((float)c, (float)-s);
+  dst[i] = make_cx((rl)c, (rl)-s);
 }
-cudaError_t launch_twiddle_table(float2* dst, i64 n, int S, int H, cudaStream_t st) {
+cudaError_t launch_twiddle_table(cx* dst, i64 n, int S, int H, cudaStream_t st) {
   const int tot = S + H;
   twiddle_table_kernel<<<(tot + 255) / 256, 256, 0, st>>>(dst, n, S, H);
   return cudaGetLastError();

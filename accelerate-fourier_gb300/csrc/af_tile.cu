@@ -20,13 +20,13 @@
 #include "af_device.cuh"
 #include "af_internal.h"
 
-namespace af {
+namespace AF_NS {
 
 // Scalars of one phase, held in registers (the descriptor lives in shared
 // memory; reading its fields inside the pass loops would re-read them).
 struct PhaseRegs {
   int n, lines, LS, ls, es, lcnt, S_log2, psh;
-  float sign;
+  rl sign;
   FastDiv lcnt_div;
 };
 
@@ -36,20 +36,20 @@ struct PhaseRegs {
 // table, the small powers w^b (b < Q <= 4) from at most two products, so
 // every twiddle is within three rounded products of table values.
 template <int R>
-__device__ __forceinline__ void apply_twiddles(float2* u, const float2* __restrict__ ptab, int S_log2, int t1,
-                                               float sign) {
+__device__ __forceinline__ void apply_twiddles(cx* u, const cx* __restrict__ ptab, int S_log2, int t1,
+                                               rl sign) {
   constexpr int Q = R <= 4 ? 2 : (R <= 9 ? 3 : 4);
-  float2 s[Q];
-  s[0] = make_float2(1.f, 0.f);
+  cx s[Q];
+  s[0] = make_cx(1.f, 0.f);
   s[1] = tw_lookup(ptab, S_log2, t1, sign);
 #pragma unroll
   for (int b = 2; b < Q; ++b) s[b] = b == 2 ? cmul(s[1], s[1]) : cmul(s[2], s[1]);
-  float2 big = s[0];
+  cx big = s[0];
 #pragma unroll
   for (int j = 1; j < R; ++j) {
     const int a = j / Q, b = j % Q;
     if (a >= 1 && b == 0) big = tw_lookup(ptab, S_log2, j * t1, sign);
-    const float2 w = a == 0 ? s[b] : (b == 0 ? big : cmul(big, s[b]));
+    const cx w = a == 0 ? s[b] : (b == 0 ? big : cmul(big, s[b]));
     u[j] = cmul(u[j], w);
   }
 }
@@ -59,9 +59,9 @@ __device__ __forceinline__ void apply_twiddles(float2* u, const float2* __restri
 // twiddles W^(j k tw_stride) (k = i mod p) and the radix-R DFT, and writes
 // (i-k)*R + k + j*p.
 template <int R, int T>
-__device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, float2* __restrict__ dst,
+__device__ __forceinline__ void stockham_pass(const cx* __restrict__ src, cx* __restrict__ dst,
                                               const PhaseRegs& ph, const PassDesc& pd,
-                                              const float2* __restrict__ ptab) {
+                                              const cx* __restrict__ ptab) {
   const int nb = ph.n / R;
   const int total = ph.lines * nb;
   const int p = pd.p, tws = pd.tw_stride;
@@ -72,7 +72,7 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
     const int i = g - l * nb;
     const int t = (int)fdiv((unsigned)l, ph.lcnt_div);
     const int base = t * ph.LS + (l - t * ph.lcnt) * ph.ls;
-    float2 u[R];
+    cx u[R];
     const int ib = base + i * ph.es;
 #pragma unroll
     for (int j = 0; j < R; ++j) u[j] = src[spd_(ib + j * nbe, ph.psh)];
@@ -89,8 +89,8 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, fl
 
 // Runs every pass of a phase; returns the buffer holding the result.
 template <int T>
-__device__ __forceinline__ float2* run_phase(float2* cur, float2* oth, const FftPhase* phs, int LS, int G,
-                                             const float2* tab, int psh) {
+__device__ __forceinline__ cx* run_phase(cx* cur, cx* oth, const FftPhase* phs, int LS, int G,
+                                             const cx* tab, int psh) {
   PhaseRegs r;
   r.psh = psh;
   r.n = phs->n;
@@ -102,7 +102,7 @@ __device__ __forceinline__ float2* run_phase(float2* cur, float2* oth, const Fft
   r.lcnt_div = phs->lcnt_div;
   r.S_log2 = phs->twS_log2;
   r.sign = phs->sign;
-  const float2* ptab = tab + phs->tw_off;
+  const cx* ptab = tab + phs->tw_off;
   const int npass = phs->npass;
   for (int p = 0; p < npass; ++p) {
     const PassDesc pd = phs->pass[p];
@@ -125,18 +125,18 @@ __device__ __forceinline__ float2* run_phase(float2* cur, float2* oth, const Fft
       case 25: stockham_pass<25, T>(cur, oth, r, pd, ptab); break;
       case 27: stockham_pass<27, T>(cur, oth, r, pd, ptab); break;
     }
-    float2* tmp = cur;
+    cx* tmp = cur;
     cur = oth;
     oth = tmp;
   }
   return cur;
 }
 
-__device__ __forceinline__ float2 gld(const TileBases& B, int buf, i64 a) {
+__device__ __forceinline__ cx gld(const TileBases& B, int buf, i64 a) {
   if (B.c[buf]) return B.c[buf][a];
-  return make_float2(B.re[buf][a], B.im[buf][a]);
+  return make_cx(B.re[buf][a], B.im[buf][a]);
 }
-__device__ __forceinline__ void gst(const TileBases& B, int buf, i64 a, float2 v) {
+__device__ __forceinline__ void gst(const TileBases& B, int buf, i64 a, cx v) {
   if (B.c[buf]) B.c[buf][a] = v;
   else { B.re[buf][a] = v.x; B.im[buf][a] = v.y; }
 }
@@ -190,9 +190,9 @@ __device__ __forceinline__ void for_tile(int G, int N, const FastDiv& Ndiv, cons
 
 // global read through the read-only data path (no launch writes an address
 // that another CTA of the same launch reads)
-__device__ __forceinline__ float2 gldr(const TileBases& B, int buf, i64 a) {
+__device__ __forceinline__ cx gldr(const TileBases& B, int buf, i64 a) {
   if (B.c[buf]) return __ldg(&B.c[buf][a]);
-  return make_float2(__ldg(&B.re[buf][a]), __ldg(&B.im[buf][a]));
+  return make_cx(__ldg(&B.re[buf][a]), __ldg(&B.im[buf][a]));
 }
 
 // Loads G lines x N elements into shared memory: `fetch(l, e, v)` issues the
@@ -200,11 +200,11 @@ __device__ __forceinline__ float2 gldr(const TileBases& B, int buf, i64 a) {
 // thread issues U fetches before writing any of them.
 template <int T, class F>
 __device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, const FastDiv& Gdiv, int line_fast,
-                                          F fetch, float2* sm) {
+                                          F fetch, cx* sm) {
   constexpr int U = 8;
   const int tot = G * N;
   for (int q0 = threadIdx.x; q0 < tot; q0 += T * U) {
-    float2 v[U];
+    cx v[U];
     int pos[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -229,12 +229,17 @@ __device__ __forceinline__ void load_tile(int G, int N, const FastDiv& Ndiv, con
 }
 
 // Asynchronous copy of G lines x N interleaved elements into shared memory
-// (cp.async, 8 bytes per element): `src(l, e)` gives the global address of
-// element e of line l, or nullptr for a zero.  No register staging: every element of the tile is in
-// flight at once.  The caller's barrier follows the wait.
-__device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc) {
+// (cp.async, one complex element per copy: 8 bytes in FP32, 16 in FP64):
+// `src(l, e)` gives the global address of element e of line l, or nullptr for
+// a zero.  No register staging: every element of the tile is in flight at
+// once.  The caller's barrier follows the wait.
+__device__ __forceinline__ void cp_async8(cx* sdst, const cx* gsrc) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+#ifdef AF_F64
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+#else
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+#endif
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -242,7 +247,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 template <int T, class F>
 __device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndiv, const FastDiv& Gdiv,
-                                                int line_fast, int LS, int psh, F src, float2* sm) {
+                                                int line_fast, int LS, int psh, F src, cx* sm) {
   const int tot = G * N;
   for (int q = threadIdx.x; q < tot; q += T) {
     int l, e;
@@ -254,26 +259,26 @@ __device__ __forceinline__ void load_tile_async(int G, int N, const FastDiv& Ndi
       l = q - e * G;
     }
     int pos = spd_(l * LS + e, psh);  // src may move the element (permuted tiles)
-    const float2* g = src(l, e, pos);
-    float2* d = sm + pos;
+    const cx* g = src(l, e, pos);
+    cx* d = sm + pos;
     if (g) cp_async8(d, g);
-    else *d = make_float2(0.f, 0.f);  // zero padding
+    else *d = make_cx(0.f, 0.f);  // zero padding
   }
   cp_async_wait_all();
 }
 
 // A global view (IoDesc) copied into registers with its base pointer resolved.
 struct IoRegs {
-  float2* c;
-  float* re;
-  float* im;
+  cx* c;
+  rl* re;
+  rl* im;
   i64 s_e, s_lo, s_hi, s_t;
   FastDiv lo_div;
   unsigned mA, mB;
   ModN m_mod;
   i64 q_lo, q_e, mN;
   const int* tab;
-  const float2* vec;
+  const cx* vec;
 };
 __device__ __forceinline__ IoRegs io_regs(const IoDesc& io, const TileBases& B, i64 base) {
   IoRegs r;
@@ -295,9 +300,9 @@ __device__ __forceinline__ IoRegs io_regs(const IoDesc& io, const TileBases& B, 
   r.vec = io.vec;
   return r;
 }
-__device__ __forceinline__ float2 rld(const IoRegs& r, i64 a) {
+__device__ __forceinline__ cx rld(const IoRegs& r, i64 a) {
   if (r.c) return __ldg(&r.c[a]);
-  return make_float2(__ldg(&r.re[a]), __ldg(&r.im[a]));
+  return make_cx(__ldg(&r.re[a]), __ldg(&r.im[a]));
 }
 __device__ __forceinline__ void rsplit(const IoRegs& r, int line, int& hi, int& lo) {
   hi = (int)fdiv((unsigned)line, r.lo_div);
@@ -311,16 +316,16 @@ __device__ __forceinline__ unsigned rgt(const IoRegs& r, int lo, int e) {
 
 struct StoreCtx {
   const TileBases* B;
-  float loss;
+  rl loss;
   int cot;
 };
 
 // final store of one element; the cotangent epilogue stores g = 2 w v with
 // w at the same address in BUF_AUX (real weights, interleaved as (w, 0)
 // pairs or a planar re plane) and adds w |v|^2 to the loss
-__device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, float2 v) {
+__device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, cx v) {
   if (sc.cot) {
-    const float w = sc.B->c[BUF_AUX] ? reinterpret_cast<const float*>(sc.B->c[BUF_AUX])[a] : sc.B->re[BUF_AUX][a];
+    const rl w = sc.B->c[BUF_AUX] ? reinterpret_cast<const rl*>(sc.B->c[BUF_AUX])[a] : sc.B->re[BUF_AUX][a];
     sc.loss += w * (v.x * v.x + v.y * v.y);
     v = cscale(v, 2.f * w);
   }
@@ -332,7 +337,7 @@ __device__ __forceinline__ void store_final(StoreCtx& sc, int buf, i64 a, float2
 // instruction cache.
 template <int T, bool GEN>
 __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it, const TileBases& B,
-                                          float2* A, float2* Bf, const float2* tab, float2* xs, double* loss) {
+                                          cx* A, cx* Bf, const cx* tab, cx* xs, double* loss) {
   const int line0 = it.line0;
   const int G = it.G;
   const int N = d.nlen;
@@ -345,7 +350,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     Gdiv.s = s;
     Gdiv.m = G <= 1 ? 0u : (unsigned)(((1ull << 32) * ((1ull << s) - (unsigned)G)) / (unsigned)G + 1);
   }
-  float2* sm = A;
+  cx* sm = A;
   const IoDesc& in = d.in;
   const IoDesc& out = d.out;
   const i64 ibase = in.off + it.in_add;
@@ -362,7 +367,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     lbo[l] = line_base(out, line0 + l);
   }
   __syncthreads();
-  float lsum = 0.f;
+  rl lsum = 0.f;
 
   // ------------------------------------------------------------ load
   // Loads are issued in groups of U independent read-only-path loads per
@@ -374,7 +379,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     switch (GEN ? in.map : (int)IO_AFFINE) {
       case IO_AFFINE:
         if (r.c) {  // interleaved: asynchronous copies straight into shared memory
-          const float2* c = r.c;
+          const cx* c = r.c;
           const i64 se = r.s_e;
           if (se == 1)
             load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) { return c + lbi[l] + e; }, sm);
@@ -382,13 +387,13 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
             load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh,
                                [&](int l, int e, int&) { return c + lbi[l] + (i64)e * se; }, sm);
         } else if (r.s_e == 1) {
-          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, cx& v) -> int {
             v = rld(r, lbi[l] + e);
             return spd_(l * LS + e, psh);
           }, sm);
         } else {
           const i64 se = r.s_e;
-          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+          load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, cx& v) -> int {
             v = rld(r, lbi[l] + (i64)e * se);
             return spd_(l * LS + e, psh);
           }, sm);
@@ -396,7 +401,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         break;
       case IO_GT:
         if (r.c) {
-          const float2* c = r.c;
+          const cx* c = r.c;
           load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) {
             int hi, lo;
             rsplit(r, line0 + l, hi, lo);
@@ -404,7 +409,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           }, sm);
           break;
         }
-        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, cx& v) -> int {
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
           v = rld(r, (i64)hi * r.s_hi + (i64)rgt(r, lo, e) * r.s_t);
@@ -413,8 +418,8 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         break;
       case IO_TABLE:  // zero beyond the table length mN
         if (r.c) {
-          const float2* c = r.c;
-          const float2* zero = nullptr;
+          const cx* c = r.c;
+          const cx* zero = nullptr;
           load_tile_async<T>(G, N, d.N_div, Gdiv, lf, LS, psh, [&](int l, int e, int&) {
             int hi, lo;
             rsplit(r, line0 + l, hi, lo);
@@ -423,21 +428,21 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
           }, sm);
           break;
         }
-        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, cx& v) -> int {
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
           const i64 q = lo * r.q_lo + e * r.q_e;
-          v = make_float2(0.f, 0.f);
+          v = make_cx(0.f, 0.f);
           if (q < r.mN) v = rld(r, (i64)hi * r.s_hi + (i64)__ldg(&r.tab[q]) * r.s_t);
           return spd_(l * LS + e, psh);
         }, sm);
         break;
       default:  // IO_CHIRP: zero pad beyond the logical length
-        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, float2& v) -> int {
+        load_tile<T>(G, N, d.N_div, Gdiv, lf, [&](int l, int e, cx& v) -> int {
           int hi, lo;
           rsplit(r, line0 + l, hi, lo);
           const i64 q = lo * r.q_lo + e * r.q_e;
-          v = make_float2(0.f, 0.f);
+          v = make_cx(0.f, 0.f);
           if (q < r.mN) v = cmul(__ldg(&r.vec[q]), rld(r, (i64)hi * r.s_hi + q * r.s_t));
           return spd_(l * LS + e, psh);
         }, sm);
@@ -454,7 +459,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     // grid position (k, j) holds x[(n k + m j) mod N]  (Planned.hs:597-606);
     // inverting: k = i*cm mod m, j = i*cn mod n
     if (B.c[in.buf]) {
-      const float2* c = B.c[in.buf];
+      const cx* c = B.c[in.buf];
       load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, psh, [&](int l, int i, int& pos) {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
@@ -464,7 +469,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         return c + io_addr_l(in, ibase, lbi[l], hi, lo, i);
       }, sm);
     } else {
-      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, float2& v) -> int {
+      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int i, cx& v) -> int {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
         const int k = (int)mulmod((unsigned)i, (unsigned)d.gt_cm, d.gt_m_mod);
@@ -480,11 +485,11 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     // a convolution carried by longer transforms (slen > p-1) is zero padded
     for (int q = threadIdx.x; q < G * (d.slen - m); q += T) {
       const int l = q / (d.slen - m);
-      sm[spd_(l * d.LS + m + (q - l * (d.slen - m)), psh)] = make_float2(0.f, 0.f);
+      sm[spd_(l * d.LS + m + (q - l * (d.slen - m)), psh)] = make_cx(0.f, 0.f);
     }
     const int xs_pos = (int)(xs - sm);  // x0 of line l goes to xs[2 l]
     if (B.c[in.buf]) {
-      const float2* c = B.c[in.buf];
+      const cx* c = B.c[in.buf];
       load_tile_async<T>(G, N, d.N_div, Gdiv, 0, d.LS, psh, [&](int l, int r, int& pos) {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
@@ -497,7 +502,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
         return c + io_addr_l(in, ibase, lbi[l], hi, lo, r);
       }, sm);
     } else {
-      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, float2& v) -> int {
+      load_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r, cx& v) -> int {
         int hi, lo;
         split_line(in, line0 + l, hi, lo);
         v = gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, r));
@@ -508,10 +513,10 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     }
   } else {  // TILE_BLUESTEIN: chirp * x zero padded to M (Planned.hs:765-773)
     const int M = d.slen;
-    load_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e, float2& v) -> int {
+    load_tile<T>(G, M, d.S_div, Gdiv, 0, [&](int l, int e, cx& v) -> int {
       int hi, lo;
       split_line(in, line0 + l, hi, lo);
-      v = make_float2(0.f, 0.f);
+      v = make_cx(0.f, 0.f);
       if (e < N) v = cmul(__ldg(&d.vec_a[e]), gldr(B, in.buf, io_addr_l(in, ibase, lbi[l], hi, lo, e)));
       return spd_(l * d.LS + e, psh);
     }, sm);
@@ -561,21 +566,21 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   StoreCtx sc{&B, 0.f, d.cot};
   if (rows_kind) {
     const IoRegs ro = io_regs(out, B, obase);
-    const float2* __restrict__ ptw = d.ptw;
+    const cx* __restrict__ ptw = d.ptw;
     const int ptwS = d.ptwS_log2;
     const ModN pmod = d.ptw_mod;
-    const float psign = d.ptw_sign;
-    const float scale = d.scale;
+    const rl psign = d.ptw_sign;
+    const rl scale = d.scale;
     const int cot = d.cot;
-    const float* __restrict__ wp = B.c[BUF_AUX] ? reinterpret_cast<const float*>(B.c[BUF_AUX]) : B.re[BUF_AUX];
+    const rl* __restrict__ wp = B.c[BUF_AUX] ? reinterpret_cast<const rl*>(B.c[BUF_AUX]) : B.re[BUF_AUX];
     const int omap = GEN ? out.map : (int)IO_AFFINE;
     // Rader scatter: x0 of transform hi and the DC slot
-    const float2* x0p = B.c[out.x0_buf] + out.x0_off + (out.x0_buf == in.buf ? it.in_add : it.out_add);
+    const cx* x0p = B.c[out.x0_buf] + out.x0_off + (out.x0_buf == in.buf ? it.in_add : it.out_add);
     const i64 x0_shi = out.x0_shi;
-    const float2* dcp = B.c[BUF_WS] + out.dc_off + it.in_add;
-    auto put = [&](i64 rel, float2 v) {
+    const cx* dcp = B.c[BUF_WS] + out.dc_off + it.in_add;
+    auto put = [&](i64 rel, cx v) {
       if (cot) {
-        const float w = __ldg(&wp[obase + rel]);
+        const rl w = __ldg(&wp[obase + rel]);
         lsum += w * (v.x * v.x + v.y * v.y);
         v = cscale(v, 2.f * w);
       }
@@ -590,12 +595,12 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       } else {
         rsplit(ro, line0 + l, hi, lo);
       }
-      float2 v = sm[spd_(l * LS + e, psh)];
+      cx v = sm[spd_(l * LS + e, psh)];
       if (ptw) {
         const unsigned t = mulmod((unsigned)lo, (unsigned)e, pmod);
-        const float2 wl = __ldg(&ptw[t & ((1u << ptwS) - 1)]);
-        const float2 wh = __ldg(&ptw[(1u << ptwS) + (t >> ptwS)]);
-        float2 w = cmul(wh, wl);
+        const cx wl = __ldg(&ptw[t & ((1u << ptwS) - 1)]);
+        const cx wh = __ldg(&ptw[(1u << ptwS) + (t >> ptwS)]);
+        cx w = cmul(wh, wl);
         w.y *= -psign;
         v = cmul(v, w);
       }
@@ -613,7 +618,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
       } else {  // IO_RADER: c[q] -> out[g^q] = x0 + c[q]; q == 0 also out[0] = x0 + dc
         const i64 q = lo * ro.q_lo + e * ro.q_e;
         if (q >= ro.mN) return;  // padding of a longer convolution
-        const float2 x0 = x0p[(i64)hi * x0_shi];
+        const cx x0 = x0p[(i64)hi * x0_shi];
         put(hb + (i64)__ldg(&ro.tab[q]) * ro.s_t, cadd(x0, v));
         if (q == 0) put(hb, cadd(x0, cscale(dcp[hi], scale)));
       }
@@ -624,7 +629,7 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 v = sm[spd_(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
+      const cx v = sm[spd_(l * d.LS + (int)mod_of((unsigned)r, d.gt_m_mod) * d.gt_n +
                                (int)mod_of((unsigned)r, d.gt_n_mod), psh)];
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(v, d.scale));
     });
@@ -633,25 +638,25 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int r) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 x0 = xs[2 * l];
-      const float2 v = r == 0 ? xs[2 * l + 1] : sm[spd_(l * d.LS + __ldg(&d.dlog[r - 1]), psh)];
+      const cx x0 = xs[2 * l];
+      const cx v = r == 0 ? xs[2 * l + 1] : sm[spd_(l * d.LS + __ldg(&d.dlog[r - 1]), psh)];
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, r), cscale(cadd(x0, v), d.scale));
     });
   } else {  // Bluestein: y = chirp * (take N c)
     for_tile<T>(G, N, d.N_div, Gdiv, 0, [&](int l, int e) {
       int hi, lo;
       split_line(out, line0 + l, hi, lo);
-      const float2 v = cmul(__ldg(&d.vec_a[e]), sm[spd_(l * d.LS + e, psh)]);
+      const cx v = cmul(__ldg(&d.vec_a[e]), sm[spd_(l * d.LS + e, psh)]);
       store_final(sc, out.buf, io_addr_l(out, obase, lbo[l], hi, lo, e), cscale(v, d.scale));
     });
   }
 
   if (d.cot && loss) {
-    float v = sc.loss;
+    rl v = sc.loss;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();  // the per-line scratch is free again: reuse it for the reduction
-    float* red = reinterpret_cast<float*>(xs);
+    rl* red = reinterpret_cast<rl*>(xs);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -662,12 +667,19 @@ __device__ __forceinline__ void tile_body(const TileDesc& d, const WorkItem& it,
   }
 }
 
+// FP32 tiles keep three 256-thread CTAs per SM; FP64 tiles (twice the
+// registers and shared memory per element) one.
+#ifdef AF_F64
+#define AF_MIN_CTAS(T) 1
+#else
+#define AF_MIN_CTAS(T) (T <= 256 ? 768 / T : 1)
+#endif
 template <int T, bool GEN>
-__global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const TileDesc* __restrict__ descs,
+__global__ void __launch_bounds__(T, AF_MIN_CTAS(T)) tile_kernel(const TileDesc* __restrict__ descs,
                                                  const WorkItem* __restrict__ items, TileBases bases,
                                                  double* loss, int smem_data) {
   extern __shared__ float4 smem4[];
-  float2* smem = reinterpret_cast<float2*>(smem4);
+  cx* smem = reinterpret_cast<cx*>(smem4);
   const WorkItem it = items[blockIdx.x];
   // shared layout: [descriptor] [A: smem_data] [B: smem_data] [tables] [scratch 4G]
   TileDesc* d = reinterpret_cast<TileDesc*>(smem);
@@ -678,22 +690,22 @@ __global__ void __launch_bounds__(T, (T <= 256 ? 768 / T : 1)) tile_kernel(const
     for (int i = threadIdx.x; i < words; i += T) dstw[i] = srcw[i];
   }
   __syncthreads();
-  const int desc_f2 = (int)((sizeof(TileDesc) + 15) / 16 * 2);
-  float2* A = smem + desc_f2;
-  float2* Bf = A + smem_data;
-  float2* tab = Bf + smem_data;
-  float2* xs = tab + d->tw_total;
+  const int desc_f2 = (int)((sizeof(TileDesc) + 15) / 16 * 16 / sizeof(cx));
+  cx* A = smem + desc_f2;
+  cx* Bf = A + smem_data;
+  cx* tab = Bf + smem_data;
+  cx* xs = tab + d->tw_total;
   // the twiddle tables travel with the tile's own asynchronous copies (one
   // wait for both, before the first pass)
   for (int i = threadIdx.x; i < d->tw_total; i += T) cp_async8(tab + i, d->tw_src + i);
   tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
-// descriptor, two buffers, tables, per-line scratch (4 float2 per line; at
-// least 8: the loss reduction keeps one float per warp there)
+// descriptor, two buffers, tables, per-line scratch (4 cx per line; at
+// least 8: the loss reduction keeps one rl per warp there)
 size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
   const int scratch = 4 * G > 8 ? 4 * G : 8;  // Rader x0/sum pairs, then the line bases
-  return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + scratch) * sizeof(float2);
+  return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + scratch) * sizeof(cx);
 }
 
 // Raises the kernel's dynamic shared-memory limit to what the device allows

@@ -104,6 +104,25 @@ af_status af_vjp_c2c(af_plan plan, af_layout layout, const float* cot_re,
                      const float* cot_im, float* grad_re, float* grad_im,
                      int64_t batch, af_stream stream);
 
+/* Complex Double ------------------------------------------------------------
+ * The reference transforms are polymorphic over the element type
+ * (`A.RealFloat a`, Planned.hs:103-106; Complex Double in its own tests,
+ * test/Test/Data/Array/Accelerate/Fourier.hs:34-35).  af_plan_create_f64
+ * builds a plan of the same reference tree whose tables, kernels and
+ * workspaces hold Complex Double (FP64 throughout).  Such a plan runs only
+ * through the _f64 entry points; the Complex Float entry points refuse it
+ * (AF_ERR_INVALID), and the other way round.  af_plan_destroy,
+ * af_plan_describe and af_plan_launches take either kind.
+ * INTERLEAVED data is double2 (16-byte aligned); PLANAR is two double arrays. */
+af_status af_plan_create_f64(af_plan* plan, int64_t n, int sign, af_algo algo);
+af_status af_exec_c2c_f64(af_plan plan, af_layout layout, const double* in_re,
+                          const double* in_im, double* out_re, double* out_im,
+                          int64_t batch, af_stream stream);
+/* Adjoint of af_exec_c2c_f64: grad = DFT^H(cot). */
+af_status af_vjp_c2c_f64(af_plan plan, af_layout layout, const double* cot_re,
+                         const double* cot_im, double* grad_re, double* grad_im,
+                         int64_t batch, af_stream stream);
+
 /* Utility.scaleDown (Fourier/Utility.hs:17-26): x *= 1/n over `batch` rows
  * of length n, in place. */
 af_status af_scale_down(af_layout layout, float* re, float* im, int64_t n,
@@ -165,6 +184,15 @@ af_status af_exec_c2c_3d(af_plan plan0, af_plan plan1, af_plan plan2,
                          af_layout layout, const float* in_re,
                          const float* in_im, float* out_re, float* out_im,
                          int64_t batch, af_stream stream);
+/* The same over Complex Double plans (af_plan_create_f64). */
+af_status af_exec_c2c_2d_f64(af_plan plan0, af_plan plan1, af_layout layout,
+                             const double* in_re, const double* in_im,
+                             double* out_re, double* out_im, int64_t batch,
+                             af_stream stream);
+af_status af_exec_c2c_3d_f64(af_plan plan0, af_plan plan1, af_plan plan2,
+                             af_layout layout, const double* in_re,
+                             const double* in_im, double* out_re,
+                             double* out_im, int64_t batch, af_stream stream);
 
 /* Real transforms (Real.hs) ------------------------------------------------
  * `half` is the plan of the half-length complex transform the reference takes

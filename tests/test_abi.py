@@ -67,6 +67,24 @@ def test_invalid_arguments_are_reported():
     assert L.af_exec_c2c(None, 0, None, None, None, None, 1, None) == _lib.AF_ERR_INVALID
 
 
+def test_invalid_arguments_of_the_f64_entry_points():
+    """Complex Double entry points: the same checks before any device work."""
+    import ctypes
+    from accelerate_fourier import _lib
+    L = _lib.load()
+    INV = _lib.AF_ERR_INVALID
+    h = ctypes.c_void_p()
+    assert L.af_plan_create_f64(ctypes.byref(h), -1, -1, 0) == INV
+    assert b"negative" in L.af_last_error()
+    assert L.af_plan_create_f64(ctypes.byref(h), 16, 2, 0) == INV
+    assert L.af_plan_create_f64(None, 16, -1, 0) == INV
+    assert L.af_plan_create_f64(ctypes.byref(h), 1 << 31, -1, 0) == _lib.AF_ERR_UNSUPPORTED
+    assert L.af_exec_c2c_f64(None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_vjp_c2c_f64(None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_exec_c2c_2d_f64(None, None, 0, None, None, None, None, 1, None) == INV
+    assert L.af_exec_c2c_3d_f64(None, None, None, 0, None, None, None, None, 1, None) == INV
+
+
 def test_invalid_arguments_of_the_other_entry_points():
     """Argument checks that fail before any device work (no GPU needed)."""
     from accelerate_fourier import _lib

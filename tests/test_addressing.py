@@ -15,29 +15,35 @@ import pytest
 def _lib():
     from accelerate_fourier import _lib
     L = _lib.load()
-    L.afx_check_plan.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p,
-                                 ctypes.c_size_t]
-    L.afx_check_plan.restype = ctypes.c_int
-    L.afx_check_axis.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
-                                 ctypes.c_char_p, ctypes.c_size_t]
-    L.afx_check_axis.restype = ctypes.c_int
+    for sfx in ("", "_f64"):
+        f = getattr(L, "afx_check_plan" + sfx)
+        f.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctypes.c_size_t]
+        f.restype = ctypes.c_int
+        f = getattr(L, "afx_check_axis" + sfx)
+        f.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_char_p,
+                      ctypes.c_size_t]
+        f.restype = ctypes.c_int
     L.afx_check_batch.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
     L.afx_check_batch.restype = ctypes.c_int
     return L, _lib.ALGO
 
 
-def check_plan(n, sign=-1, algo="auto", batch=1):
+def check_plan(n, sign=-1, algo="auto", batch=1, double=False):
+    """double: the programs of the Complex Double engine (smaller tiles, so
+    other splits), checked by its own build of the checker."""
     L, ALGO = _lib()
     msg = ctypes.create_string_buffer(1024)
-    rc = L.afx_check_plan(n, sign, ALGO[algo], batch, msg, len(msg))
-    assert rc == 0, (n, algo, batch, msg.value.decode())
+    f = L.afx_check_plan_f64 if double else L.afx_check_plan
+    rc = f(n, sign, ALGO[algo], batch, msg, len(msg))
+    assert rc == 0, (n, algo, batch, double, msg.value.decode())
 
 
-def check_axis(n, outer, inner, sign=-1, algo="auto"):
+def check_axis(n, outer, inner, sign=-1, algo="auto", double=False):
     L, ALGO = _lib()
     msg = ctypes.create_string_buffer(1024)
-    rc = L.afx_check_axis(n, sign, ALGO[algo], outer, inner, msg, len(msg))
-    assert rc == 0, (n, outer, inner, msg.value.decode())
+    f = L.afx_check_axis_f64 if double else L.afx_check_axis
+    rc = f(n, sign, ALGO[algo], outer, inner, msg, len(msg))
+    assert rc == 0, (n, outer, inner, double, msg.value.decode())
 
 
 def check_batch(sizes, sign=-1):
@@ -94,3 +100,25 @@ def test_axis_addressing(n):
         if n * outer * inner <= (1 << 23):
             check_axis(n, outer, inner)
     check_axis(n, 2, 3, sign=1)
+
+
+# Complex Double programs: tiles hold at most 6200 elements, so lengths
+# between that and 13000 take the multi-pass schemes in FP64
+@pytest.mark.parametrize("n", SIZES + [6144, 6200, 6201, 6250, 7776, 9973, 10007, 12289 * 2])
+def test_plan_addressing_f64(n):
+    check_plan(n, -1, "auto", 1, double=True)
+    if n <= 20000:
+        check_plan(n, 1, "auto", 3, double=True)
+
+
+def test_algorithm_addressing_f64():
+    for algo in ["decompose", "chirp2", "chirp235", "adhoc_auto"]:
+        for n in [2, 3, 17, 100, 1009, 4099, 16385, 30011]:
+            check_plan(n, -1, algo, 2, double=True)
+
+
+@pytest.mark.parametrize("n", [1, 16, 17, 100, 1001, 4096, 6250, 16384, 30011, 65537])
+def test_axis_addressing_f64(n):
+    for outer, inner in [(1, 1), (1, 7), (3, 5), (2, 64)]:
+        if n * outer * inner <= (1 << 22):
+            check_axis(n, outer, inner, double=True)
