@@ -34,7 +34,7 @@ for _p in (ROOT, os.path.join(ROOT, "accelerate-fourier_gb300")):
 METRIC = "C2C FFT GB/s & % HBM roofline (fwd+VJP, batched mixed N) vs plain; err vs FP64"
 UNIT = "GB/s"
 COUNT = 4096
-STEP_DRAM_BYTES = 2.696e9  # DRAM bytes per step of the default workload (ncu, see the profiles)
+STEP_DRAM_BYTES = 2.667e9  # DRAM bytes per step of the default workload (ncu, see the profiles)
 
 
 # ----------------------------------------------------------------- workload
