@@ -43,6 +43,21 @@ SIGNATURES = {
     "af_vjp_c2c_f64": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_exec_c2c_2d_f64": ([PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_exec_c2c_3d_f64": ([PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_exec_c2c_axis_f64": ([PTR, INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_scale_down_f64": ([INT, PTR, PTR, I64, I64, PTR], INT),
+    "af_cyclic_reverse_f64": ([INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_cyclic_reverse_2d_f64": ([INT, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
+    "af_to_spectrum_f64": ([PTR, PTR, INT, INT, PTR, PTR, I64, PTR], INT),
+    "af_from_spectrum_f64": ([PTR, INT, PTR, PTR, PTR, I64, PTR], INT),
+    "af_vjp_to_spectrum_f64": ([PTR, INT, PTR, PTR, PTR, I64, PTR], INT),
+    "af_untangle_spectra_f64": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_untangle_spectra_2d_f64": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
+    "af_entangle_spectra_f64": ([INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
+    "af_two_to_spectrum_f64": ([PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_to_spectrum_2d_f64": ([PTR, PTR, PTR, PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_from_spectrum_f64": ([PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_two_from_spectrum_2d_f64": ([PTR, PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
+    "af_convolve_cyclic_f64": ([PTR, INT, PTR, PTR, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_vjp_c2c": ([PTR, INT, PTR, PTR, PTR, PTR, I64, PTR], INT),
     "af_scale_down": ([INT, PTR, PTR, I64, I64, PTR], INT),
     "af_cyclic_reverse": ([INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),

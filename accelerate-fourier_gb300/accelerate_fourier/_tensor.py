@@ -44,6 +44,25 @@ def is_double(x) -> bool:
     return x.dtype == torch.complex128
 
 
+def cdtype(double: bool):
+    return torch.complex128 if double else torch.complex64
+
+
+def rdtype(double: bool):
+    return torch.float64 if double else torch.float32
+
+
+def as_complex(x: torch.Tensor, double: bool) -> torch.Tensor:
+    """x as a contiguous complex64 (or complex128) CUDA tensor."""
+    require_cuda(x)
+    return x.to(cdtype(double)).contiguous()
+
+
+def fn(name: str, double: bool):
+    """The C entry point `name`, or its Complex Double form `name_f64`."""
+    return getattr(_lib.load(), name + ("_f64" if double else ""))
+
+
 def run_plan(plan: "_lib.Plan", x, vjp: bool = False, out=None):
     """Apply an af_plan to the last axis of x (complex64 tensor or (re, im);
     complex128 or float64 pairs for a Complex Double plan)."""

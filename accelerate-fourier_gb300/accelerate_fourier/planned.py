@@ -29,9 +29,11 @@ class Transform:
         self.plan = _plan(self.sign, self.length, algo)
 
     def plan_for(self, x) -> _lib.Plan:
-        if _tensor.is_double(x):
-            return _plan(self.sign, self.length, self.algo, True)
-        return self.plan
+        return self.plan_of(_tensor.is_double(x))
+
+    def plan_of(self, double: bool) -> _lib.Plan:
+        """The plan of this transform over Complex Double (double) or Complex Float."""
+        return _plan(self.sign, self.length, self.algo, True) if double else self.plan
 
     def __call__(self, x, out=None):
         return _tensor.run_plan(self.plan_for(x), x, out=out)
@@ -90,7 +92,7 @@ class TransformND:
             raise ValueError("TransformND takes two or three transforms")
         self.transforms = transforms
 
-    def shape_check(self, shape):
+    def shape_check(self, shape, double: bool = False):
         d = len(self.transforms)
         if len(shape) < d:
             raise ValueError(f"array needs at least {d} axes")
@@ -103,7 +105,7 @@ class TransformND:
         batch = 1
         for s in shape[:-d]:
             batch *= int(s)
-        return (*[t.plan for t in self.transforms], batch)
+        return (*[t.plan_of(double) for t in self.transforms], batch)
 
     def __call__(self, x, out=None):
         import torch
@@ -140,15 +142,19 @@ class TransformND:
 
 def convolveCyclic(length: int):
     """Planned.convolveCyclic (Planned.hs:779-790): a function of two complex
-    arrays of the given length, F(G(x)/n * G(y)) with the planned transforms."""
+    arrays of the given length, F(G(x)/n * G(y)) with the planned transforms.
+    complex128 (or float64 planes) runs in Complex Double."""
     t = Transform(forward, length, "auto")
 
     def conv(x, y):
         import torch
         if isinstance(x, tuple) != isinstance(y, tuple):
             raise ValueError("x and y must have one layout")
+        double = _tensor.is_double(x)
+        f = _tensor.fn("af_convolve_cyclic", double)
+        h = t.plan_of(double).handle
         if isinstance(x, tuple):
-            xr, xi, yr, yi = (a.contiguous().to(torch.float32) for a in (*x, *y))
+            xr, xi, yr, yi = (a.contiguous().to(_tensor.rdtype(double)) for a in (*x, *y))
             _tensor.require_cuda(xr)
             if xr.shape != yr.shape:
                 raise ValueError("signals must have equal size")
@@ -157,11 +163,10 @@ def convolveCyclic(length: int):
                 raise ValueError("length mismatch")
             ore, oim = torch.empty_like(xr), torch.empty_like(xi)
             if xr.numel():
-                _lib.check(_lib.load().af_convolve_cyclic(t.plan.handle, _lib.PLANAR, xr.data_ptr(), xi.data_ptr(),
-                                                          yr.data_ptr(), yi.data_ptr(), ore.data_ptr(),
-                                                          oim.data_ptr(), batch, _tensor.stream_ptr()))
+                _lib.check(f(h, _lib.PLANAR, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(),
+                             ore.data_ptr(), oim.data_ptr(), batch, _tensor.stream_ptr()))
             return ore, oim
-        x, y = _tensor.as_c64(x), _tensor.as_c64(y)
+        x, y = _tensor.as_complex(x, double), _tensor.as_complex(y, double)
         if x.shape != y.shape:
             raise ValueError("signals must have equal size")
         n, batch = _tensor.rows(x)
@@ -169,9 +174,8 @@ def convolveCyclic(length: int):
             raise ValueError("length mismatch")
         out = torch.empty_like(x)
         if x.numel():
-            _lib.check(_lib.load().af_convolve_cyclic(t.plan.handle, _lib.INTERLEAVED, x.data_ptr(), None,
-                                                      y.data_ptr(), None, out.data_ptr(), None, batch,
-                                                      _tensor.stream_ptr()))
+            _lib.check(f(h, _lib.INTERLEAVED, x.data_ptr(), None, y.data_ptr(), None, out.data_ptr(), None, batch,
+                         _tensor.stream_ptr()))
         return out
 
     return conv

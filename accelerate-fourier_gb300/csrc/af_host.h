@@ -10,7 +10,6 @@
 #include "../../include/af.h"
 #include "af_internal.h"
 #include "af_plan.h"
-#include "af_f64.h"
 
 // Shared by both precisions of the engine.
 namespace af {
@@ -145,21 +144,43 @@ const void* batch_res(BatchPlan* B);
 
 }  // namespace af
 
-#ifndef AF_F64
+// Per-precision state of a plan (defined below for this build's precision;
+// both precisions' functions are visible to the shared C ABI code).
+struct af_plan_s;
+namespace af {
+struct PlanState;
+void state_destroy(PlanState* s);
+long long state_launches(af_plan_s* P, long long batch);
+}  // namespace af
+namespace af64 {
+struct PlanState;
+void state_destroy(PlanState* s);
+long long state_launches(af_plan_s* P, long long batch);
+}  // namespace af64
+
+namespace AF_NS {
+// Tables, programs and buffers of a plan in one precision.
+struct PlanState {
+  PlanRes res;
+  std::map<std::pair<long long, int>, Program> progs;                        // (batch, sign)
+  std::map<std::tuple<long long, long long, int>, Program> axis_progs;  // (outer, inner, sign)
+  cx* ws = nullptr;
+  size_t ws_elems = 0;
+  cx* stage = nullptr;  // staging for the real transforms and convolutions
+  size_t stage_elems = 0;
+  ~PlanState();
+};
+}  // namespace AF_NS
+
+// The object behind an af_plan: the reference plan tree, and the state of the
+// precision it was created for (af_plan_create: s32, af_plan_create_f64: s64).
 struct af_plan_s {
   long long n = 0;
   int sign = -1;
   int algo = 0;
   af::Planner planner;
   const af::Node* root = nullptr;
-  af::PlanRes res;
-  std::map<std::pair<long long, int>, af::Program> progs;  // (batch, sign)
-  std::map<std::tuple<long long, long long, int>, af::Program> axis_progs;  // (outer, inner, sign)
-  float2* ws = nullptr;
-  size_t ws_elems = 0;
-  float2* stage = nullptr;  // staging for the real transforms and convolutions
-  size_t stage_elems = 0;
-  af64::Plan* p64 = nullptr;  // set for a Complex Double plan (af_plan_create_f64)
+  af::PlanState* s32 = nullptr;
+  af64::PlanState* s64 = nullptr;
   ~af_plan_s();
 };
-#endif

@@ -4,17 +4,17 @@
 // product of the cyclic convolution (Planned.hs:779-821).
 #include "af_internal.h"
 
-namespace af {
+namespace AF_NS {
 
-__device__ __forceinline__ float2 cp_ld(const CPtr& p, i64 i) {
+__device__ __forceinline__ cx cp_ld(const CPtr& p, i64 i) {
   if (p.c) return p.c[i];
-  return make_float2(p.re[i], p.im[i]);
+  return make_cx(p.re[i], p.im[i]);
 }
-__device__ __forceinline__ void cp_st(const CPtr& p, i64 i, float2 v) {
+__device__ __forceinline__ void cp_st(const CPtr& p, i64 i, cx v) {
   if (p.c) p.c[i] = v;
   else { p.re[i] = v.x; p.im[i] = v.y; }
 }
-__device__ __forceinline__ float2 i_times(float2 a) { return make_float2(-a.y, a.x); }
+__device__ __forceinline__ cx i_times(cx a) { return make_cx(-a.y, a.x); }
 
 static unsigned grid_of(i64 total) {
   i64 b = (total + 255) / 256;
@@ -28,17 +28,17 @@ static unsigned grid_of(i64 total) {
 //   even = Re xp + i Im xm, odd = (i W_N^k) (Re xm + i Im xp)
 //   out = (even - odd) ++ (even + odd)           (nout = N)
 // With nout = n2 + 1 only the first half and the Nyquist bin are written.
-__global__ void real_untangle_kernel(const float2* __restrict__ Z, CPtr out, i64 n2, i64 nout, i64 rows,
-                                     const float2* __restrict__ tab, int S_log2) {
+__global__ void real_untangle_kernel(const cx* __restrict__ Z, CPtr out, i64 n2, i64 nout, i64 rows,
+                                     const cx* __restrict__ tab, int S_log2) {
   const i64 total = rows * n2;
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
     const i64 b = q / n2, k = q - b * n2;
-    const float2* z = Z + b * n2;
-    const float2 zk = z[k], zr = z[k == 0 ? 0 : n2 - k];
-    const float2 xp = cscale(cadd(zk, zr), 0.5f), xm = cscale(csub(zk, zr), 0.5f);
-    const float2 ev = make_float2(xp.x, xm.y);
-    const float2 oi = make_float2(xm.x, xp.y);
-    const float2 od = cmul(i_times(tw_lookup(tab, S_log2, (int)k, -1.f)), oi);
+    const cx* z = Z + b * n2;
+    const cx zk = z[k], zr = z[k == 0 ? 0 : n2 - k];
+    const cx xp = cscale(cadd(zk, zr), 0.5f), xm = cscale(csub(zk, zr), 0.5f);
+    const cx ev = make_cx(xp.x, xm.y);
+    const cx oi = make_cx(xm.x, xp.y);
+    const cx od = cmul(i_times(tw_lookup(tab, S_log2, (int)k, -1.f)), oi);
     cp_st(out, b * nout + k, csub(ev, od));
     if (nout == 2 * n2) cp_st(out, b * nout + n2 + k, cadd(ev, od));
     else if (k == 0) cp_st(out, b * nout + n2, cadd(ev, od));
@@ -50,21 +50,21 @@ __global__ void real_untangle_kernel(const float2* __restrict__ Z, CPtr out, i64
 // transform of n2 and is read back as N reals.  With herm != 0 the spectrum
 // is first made self-adjoint, s = (g + conj(rev g))/2: that turns the map
 // into the adjoint of toSpectrum (Re(DFT^H g) = fromSpectrum(s)).
-__global__ void real_entangle_kernel(CPtr spec, float2* __restrict__ f, i64 n2, i64 rows,
-                                     const float2* __restrict__ tab, int S_log2, int herm) {
+__global__ void real_entangle_kernel(CPtr spec, cx* __restrict__ f, i64 n2, i64 rows,
+                                     const cx* __restrict__ tab, int S_log2, int herm) {
   const i64 total = rows * n2, N = 2 * n2;
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
     const i64 b = q / n2, k = q - b * n2;
     const i64 row = b * N;
-    float2 s0 = cp_ld(spec, row + k), s1 = cp_ld(spec, row + k + n2);
+    cx s0 = cp_ld(spec, row + k), s1 = cp_ld(spec, row + k + n2);
     if (herm) {
-      const float2 r0 = cp_ld(spec, row + (k == 0 ? 0 : N - k));
-      const float2 r1 = cp_ld(spec, row + (n2 - k));
+      const cx r0 = cp_ld(spec, row + (k == 0 ? 0 : N - k));
+      const cx r1 = cp_ld(spec, row + (n2 - k));
       s0 = cscale(cadd(s0, conjf2(r0)), 0.5f);
       s1 = cscale(cadd(s1, conjf2(r1)), 0.5f);
     }
-    const float2 fe = cadd(s0, s1);
-    const float2 fo = cmul(i_times(tw_lookup(tab, S_log2, (int)k, 1.f)), csub(s0, s1));
+    const cx fe = cadd(s0, s1);
+    const cx fo = cmul(i_times(tw_lookup(tab, S_log2, (int)k, 1.f)), csub(s0, s1));
     f[b * n2 + k] = cadd(fe, fo);
   }
 }
@@ -78,11 +78,11 @@ __global__ void untangle_kernel(CPtr S, CPtr A, CPtr B, i64 h, i64 w, i64 total)
     const i64 bi = q / img, r = q - bi * img;
     const i64 y = r / w, x = r - y * w;
     const i64 ry = y == 0 ? 0 : h - y, rx = x == 0 ? 0 : w - x;
-    const float2 a = cp_ld(S, q);
-    const float2 bc = conjf2(cp_ld(S, bi * img + ry * w + rx));
+    const cx a = cp_ld(S, q);
+    const cx bc = conjf2(cp_ld(S, bi * img + ry * w + rx));
     cp_st(A, q, cscale(cadd(a, bc), 0.5f));
-    const float2 d = csub(a, bc);
-    cp_st(B, q, make_float2(0.5f * d.y, -0.5f * d.x));
+    const cx d = csub(a, bc);
+    cp_st(B, q, make_cx(0.5f * d.y, -0.5f * d.x));
   }
 }
 
@@ -101,25 +101,25 @@ __global__ void reverse2d_kernel(CPtr in, CPtr out, i64 h, i64 w, i64 total) {
 // entangleCoefficient).
 __global__ void entangle_kernel(CPtr C, CPtr D, CPtr out, i64 total) {
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x) {
-    const float2 c = cp_ld(C, q), d = cp_ld(D, q);
+    const cx c = cp_ld(C, q), d = cp_ld(D, q);
     cp_st(out, q, cadd(c, i_times(d)));
   }
 }
 
 // convolveCyclicCache (Planned.hs:793-821): gx = (gx * (1/n)) * gy.
-__global__ void conv_mul_kernel(float2* __restrict__ gx, const float2* __restrict__ gy, float s, i64 total) {
+__global__ void conv_mul_kernel(cx* __restrict__ gx, const cx* __restrict__ gy, rl s, i64 total) {
   for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (i64)gridDim.x * blockDim.x)
     gx[q] = cmul(cscale(gx[q], s), gy[q]);
 }
 
-cudaError_t launch_real_untangle(const float2* Z, CPtr out, i64 n2, i64 nout, i64 rows, const float2* tab,
+cudaError_t launch_real_untangle(const cx* Z, CPtr out, i64 n2, i64 nout, i64 rows, const cx* tab,
                                  int S_log2, cudaStream_t st) {
   const i64 total = rows * n2;
   if (total <= 0) return cudaSuccess;
   real_untangle_kernel<<<grid_of(total), 256, 0, st>>>(Z, out, n2, nout, rows, tab, S_log2);
   return cudaGetLastError();
 }
-cudaError_t launch_real_entangle(CPtr spec, float2* f, i64 n2, i64 rows, const float2* tab, int S_log2, int herm,
+cudaError_t launch_real_entangle(CPtr spec, cx* f, i64 n2, i64 rows, const cx* tab, int S_log2, int herm,
                                  cudaStream_t st) {
   const i64 total = rows * n2;
   if (total <= 0) return cudaSuccess;
@@ -141,7 +141,7 @@ cudaError_t launch_entangle(CPtr C, CPtr D, CPtr out, i64 total, cudaStream_t st
   entangle_kernel<<<grid_of(total), 256, 0, st>>>(C, D, out, total);
   return cudaGetLastError();
 }
-cudaError_t launch_conv_mul(float2* gx, const float2* gy, float s, i64 total, cudaStream_t st) {
+cudaError_t launch_conv_mul(cx* gx, const cx* gy, rl s, i64 total, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   conv_mul_kernel<<<grid_of(total), 256, 0, st>>>(gx, gy, s, total);
   return cudaGetLastError();

@@ -322,6 +322,75 @@ af_status af_conv_complex_f64(int cyclic, const double* x_re, const double* x_im
 af_status af_exec_c2c_noalloc(int64_t n, int sign, const float* in, float* out,
                               int64_t batch, af_stream stream);
 
+/* The Complex Double forms of the other entry points that carry complex or
+ * real floating-point data, with the meaning, arguments and errors of the
+ * Complex Float entry point of the same name without _f64.  The plan
+ * arguments are Complex Double plans (af_plan_create_f64); the real arrays of
+ * the real and two-real transforms are double. */
+af_status af_exec_c2c_axis_f64(af_plan plan, af_layout layout,
+                               const double* in_re, const double* in_im,
+                               double* out_re, double* out_im, int64_t outer,
+                               int64_t inner, af_stream stream);
+af_status af_scale_down_f64(af_layout layout, double* re, double* im, int64_t n,
+                            int64_t batch, af_stream stream);
+af_status af_cyclic_reverse_f64(af_layout layout, const double* in_re,
+                                const double* in_im, double* out_re,
+                                double* out_im, int64_t n, int64_t batch,
+                                af_stream stream);
+af_status af_cyclic_reverse_2d_f64(af_layout layout, const double* in_re,
+                                   const double* in_im, double* out_re,
+                                   double* out_im, int64_t height,
+                                   int64_t width, int64_t batch,
+                                   af_stream stream);
+af_status af_to_spectrum_f64(af_plan half, const double* x,
+                             af_spectrum spectrum, af_layout layout,
+                             double* out_re, double* out_im, int64_t batch,
+                             af_stream stream);
+af_status af_from_spectrum_f64(af_plan half, af_layout layout,
+                               const double* spec_re, const double* spec_im,
+                               double* x, int64_t batch, af_stream stream);
+af_status af_vjp_to_spectrum_f64(af_plan half, af_layout layout,
+                                 const double* cot_re, const double* cot_im,
+                                 double* grad, int64_t batch, af_stream stream);
+af_status af_untangle_spectra_f64(af_layout layout, const double* s_re,
+                                  const double* s_im, double* a_re,
+                                  double* a_im, double* b_re, double* b_im,
+                                  int64_t n, int64_t batch, af_stream stream);
+af_status af_untangle_spectra_2d_f64(af_layout layout, const double* s_re,
+                                     const double* s_im, double* a_re,
+                                     double* a_im, double* b_re, double* b_im,
+                                     int64_t height, int64_t width,
+                                     int64_t batch, af_stream stream);
+af_status af_entangle_spectra_f64(af_layout layout, const double* c_re,
+                                  const double* c_im, const double* d_re,
+                                  const double* d_im, double* out_re,
+                                  double* out_im, int64_t n, int64_t batch,
+                                  af_stream stream);
+af_status af_two_to_spectrum_f64(af_plan plan, const double* f, const double* g,
+                                 af_layout layout, double* a_re, double* a_im,
+                                 double* b_re, double* b_im, int64_t batch,
+                                 af_stream stream);
+af_status af_two_to_spectrum_2d_f64(af_plan plan0, af_plan plan1,
+                                    const double* f, const double* g,
+                                    af_layout layout, double* a_re,
+                                    double* a_im, double* b_re, double* b_im,
+                                    int64_t batch, af_stream stream);
+af_status af_two_from_spectrum_f64(af_plan plan, af_layout layout,
+                                   const double* a_re, const double* a_im,
+                                   const double* b_re, const double* b_im,
+                                   double* f, double* g, int64_t batch,
+                                   af_stream stream);
+af_status af_two_from_spectrum_2d_f64(af_plan plan0, af_plan plan1,
+                                      af_layout layout, const double* a_re,
+                                      const double* a_im, const double* b_re,
+                                      const double* b_im, double* f, double* g,
+                                      int64_t batch, af_stream stream);
+af_status af_convolve_cyclic_f64(af_plan plan, af_layout layout,
+                                 const double* x_re, const double* x_im,
+                                 const double* y_re, const double* y_im,
+                                 double* out_re, double* out_im, int64_t batch,
+                                 af_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -175,3 +175,88 @@ def test_f64_and_f32_plans_refuse_each_other():
                              None) == _lib.AF_ERR_INVALID
     n = ctypes.c_int64()
     assert L.af_plan_launches(p64.handle, 4, ctypes.byref(n)) == 0 and n.value >= 1
+
+
+# ---------------------------------------------------------------- real, two-real, convolution, maps
+def f64(x):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x, dtype=np.float64))).cuda()
+
+
+@pytest.mark.parametrize("N", [2, 6, 64, 1000, 2 * 1009, 2 * 4099, 2 * 65537, 1 << 18])
+def test_f64_to_from_spectrum(N):
+    from accelerate_fourier import real
+    rng = np.random.default_rng(N)
+    x = rng.standard_normal((2, N))
+    sub = transform(-1, N // 2)
+    y = host(real.toSpectrum(sub, f64(x)))
+    assert y.dtype == np.complex128
+    ref = np.fft.fft(x, axis=-1)
+    assert rel_l2(y, ref) <= fp64_bound(N)
+    # the oracle's chirp phases carry about eps64 * N (see test_f64_planned_vs_oracle)
+    chirp = 8 * 2.0 ** -53 * N if "BL" in sub.describe() else 0.0
+    assert rel_l2(y, O().to_spectrum(x)) <= fp64_bound(N) + chirp
+    yh = host(real.toSpectrum(sub, f64(x), half=True))
+    assert rel_l2(yh, ref[:, : N // 2 + 1]) <= fp64_bound(N)
+    # fromSpectrum (unscaled inverse) of the full spectrum: N x
+    z = host(real.fromSpectrum(transform(1, N // 2), dev(ref)))
+    assert z.dtype == np.float64
+    assert rel_l2(z, N * x) <= fp64_bound(N)
+    # VJP of toSpectrum: Re(DFT^H g)
+    g = crand(rng, (2, N))
+    v = host(real.toSpectrum_vjp(sub, dev(g)))
+    assert rel_l2(v, (np.fft.ifft(g, axis=-1) * N).real) <= fp64_bound(N)
+
+
+@pytest.mark.parametrize("n", [1, 7, 100, 1009, 4096])
+def test_f64_two_real(n):
+    from accelerate_fourier import real
+    rng = np.random.default_rng(n)
+    f, g = rng.standard_normal((3, n)), rng.standard_normal((3, n))
+    t = transform(-1, n)
+    a, b = real.twoToSpectrum(t, (f64(f), f64(g)))
+    a, b = host(a), host(b)
+    assert rel_l2(a, np.fft.fft(f, axis=-1)) <= fp64_bound(n)
+    assert rel_l2(b, np.fft.fft(g, axis=-1)) <= fp64_bound(n)
+    ff, gg = real.twoFromSpectrum(transform(1, n), (dev(a), dev(b)))
+    assert rel_l2(host(ff), n * f) <= fp64_bound(n) and rel_l2(host(gg), n * g) <= fp64_bound(n)
+    # untangle / entangle are inverse element-wise maps
+    s = crand(rng, (3, n))
+    u, w = real.untangleSpectra(dev(s))
+    back = host(real.entangleSpectra((u, w)))
+    assert rel_l2(back, s) <= 1e-15
+
+
+def test_f64_two_real_2d():
+    from accelerate_fourier import planned, real
+    rng = np.random.default_rng(9)
+    f, g = rng.standard_normal((2, 24, 30)), rng.standard_normal((2, 24, 30))
+    t2 = planned.TransformND(transform(-1, 30), transform(-1, 24))
+    a, b = real.twoToSpectrum2d(t2, (f64(f), f64(g)))
+    assert rel_l2(host(a), np.fft.fft2(f)) <= fp64_bound(720)
+    assert rel_l2(host(b), np.fft.fft2(g)) <= fp64_bound(720)
+
+
+@pytest.mark.parametrize("n", [1, 12, 1000, 4099, 1 << 16])
+def test_f64_convolve_cyclic(n):
+    from accelerate_fourier import planned
+    rng = np.random.default_rng(n)
+    x, y = crand(rng, (2, n)), crand(rng, (2, n))
+    z = host(planned.convolveCyclic(n)(dev(x), dev(y)))
+    ref = np.fft.ifft(np.fft.fft(x, axis=-1) * np.fft.fft(y, axis=-1), axis=-1)
+    assert z.dtype == np.complex128
+    assert rel_l2(z, ref) <= fp64_bound(n)
+    zp = planned.convolveCyclic(n)((f64(x.real), f64(x.imag)), (f64(y.real), f64(y.imag)))
+    assert rel_l2(host(zp[0]) + 1j * host(zp[1]), ref) <= fp64_bound(n)
+
+
+def test_f64_reverse_and_scale_down():
+    from accelerate_fourier import cyclic, utility
+    rng = np.random.default_rng(4)
+    x = crand(rng, (3, 17, 10))
+    r = host(cyclic.reverse(dev(x)))
+    assert np.array_equal(r, np.roll(x[..., ::-1], 1, axis=-1))
+    r2 = host(cyclic.reverse2d(dev(x)))
+    assert np.array_equal(r2, np.roll(np.roll(x[..., ::-1, ::-1], 1, axis=-1), 1, axis=-2))
+    s = host(utility.scaleDown(dev(x)))
+    assert s.dtype == np.complex128
+    np.testing.assert_allclose(s, x / 10, rtol=4e-16, atol=0)
