@@ -234,15 +234,14 @@ af_status AFN(af_plan_create)(af_plan* plan, int64_t n, int sign, af_algo algo) 
   AF_CATCH
 }
 
-
-af_status AFN(af_exec_c2c)(af_plan plan, af_layout layout, const rl* in_re, const rl* in_im, rl* out_re,
-                      rl* out_im, int64_t batch, af_stream stream) {
+af_status AFN(af_exec_c2c)(af_plan plan, af_layout layout, const rl* in_re, const rl* in_im, rl* out_re, rl* out_im,
+                           int64_t batch, af_stream stream) {
   if (!plan) return fail(AF_ERR_INVALID, "null plan");
   return exec_sign(plan, plan->sign, layout, in_re, in_im, out_re, out_im, batch, stream);
 }
 
 af_status AFN(af_vjp_c2c)(af_plan plan, af_layout layout, const rl* cot_re, const rl* cot_im, rl* grad_re,
-                     rl* grad_im, int64_t batch, af_stream stream) {
+                          rl* grad_im, int64_t batch, af_stream stream) {
   if (!plan) return fail(AF_ERR_INVALID, "null plan");
   return exec_sign(plan, -plan->sign, layout, cot_re, cot_im, grad_re, grad_im, batch, stream);
 }
@@ -262,7 +261,7 @@ af_status AFN(af_scale_down)(af_layout layout, rl* re, rl* im, int64_t n, int64_
 }
 
 af_status AFN(af_cyclic_reverse)(af_layout layout, const rl* in_re, const rl* in_im, rl* out_re, rl* out_im,
-                            int64_t n, int64_t batch, af_stream stream) {
+                                 int64_t n, int64_t batch, af_stream stream) {
   AF_TRY
   if (n < 0 || batch < 0) return fail(AF_ERR_INVALID, "negative size");
   if (n == 0 || batch == 0) return AF_OK;
@@ -279,7 +278,7 @@ af_status AFN(af_cyclic_reverse)(af_layout layout, const rl* in_re, const rl* in
 
 
 af_status AFN(af_exec_c2c_axis)(af_plan plan, af_layout layout, const rl* in_re, const rl* in_im, rl* out_re,
-                           rl* out_im, int64_t outer, int64_t inner, af_stream stream) {
+                                rl* out_im, int64_t outer, int64_t inner, af_stream stream) {
   AF_TRY
   if (!plan) return fail(AF_ERR_INVALID, "null plan");
   if (outer < 0 || inner < 0) return fail(AF_ERR_INVALID, "negative size");
@@ -293,7 +292,7 @@ af_status AFN(af_exec_c2c_axis)(af_plan plan, af_layout layout, const rl* in_re,
 }
 
 af_status AFN(af_exec_c2c_2d)(af_plan plan0, af_plan plan1, af_layout layout, const rl* in_re, const rl* in_im,
-                         rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
+                              rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
   AF_TRY
   if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
   af_plan_s* plans[2] = {plan0, plan1};
@@ -307,7 +306,7 @@ af_status AFN(af_exec_c2c_2d)(af_plan plan0, af_plan plan1, af_layout layout, co
 }
 
 af_status AFN(af_exec_c2c_3d)(af_plan plan0, af_plan plan1, af_plan plan2, af_layout layout, const rl* in_re,
-                         const rl* in_im, rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
+                              const rl* in_im, rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
   AF_TRY
   if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
   af_plan_s* plans[3] = {plan0, plan1, plan2};
@@ -321,7 +320,7 @@ af_status AFN(af_exec_c2c_3d)(af_plan plan0, af_plan plan1, af_plan plan2, af_la
 }
 
 af_status AFN(af_to_spectrum)(af_plan half, const rl* x, af_spectrum spectrum, af_layout layout, rl* out_re,
-                         rl* out_im, int64_t batch, af_stream stream) {
+                              rl* out_im, int64_t batch, af_stream stream) {
   AF_TRY
   if (!half) return fail(AF_ERR_INVALID, "null plan");
   if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
@@ -367,18 +366,17 @@ static af_status from_spectrum_impl(af_plan half, af_layout layout, const rl* s_
 }
 
 af_status AFN(af_from_spectrum)(af_plan half, af_layout layout, const rl* spec_re, const rl* spec_im, rl* x,
-                           int64_t batch, af_stream stream) {
+                                int64_t batch, af_stream stream) {
   return from_spectrum_impl(half, layout, spec_re, spec_im, x, batch, stream, false);
 }
 
 af_status AFN(af_vjp_to_spectrum)(af_plan half, af_layout layout, const rl* cot_re, const rl* cot_im, rl* grad,
-                             int64_t batch, af_stream stream) {
+                                  int64_t batch, af_stream stream) {
   return from_spectrum_impl(half, layout, cot_re, cot_im, grad, batch, stream, true);
 }
 
-af_status AFN(af_untangle_spectra_2d)(af_layout layout, const rl* s_re, const rl* s_im, rl* a_re, rl* a_im,
-                                 rl* b_re, rl* b_im, int64_t height, int64_t width, int64_t batch,
-                                 af_stream stream) {
+af_status AFN(af_untangle_spectra_2d)(af_layout layout, const rl* s_re, const rl* s_im, rl* a_re, rl* a_im, rl* b_re,
+                                      rl* b_im, int64_t height, int64_t width, int64_t batch, af_stream stream) {
   AF_TRY
   if (height < 0 || width < 0 || batch < 0) return fail(AF_ERR_INVALID, "negative size");
   const i64 total = height * width * batch;
@@ -393,13 +391,13 @@ af_status AFN(af_untangle_spectra_2d)(af_layout layout, const rl* s_re, const rl
   AF_CATCH
 }
 
-af_status AFN(af_untangle_spectra)(af_layout layout, const rl* s_re, const rl* s_im, rl* a_re, rl* a_im,
-                              rl* b_re, rl* b_im, int64_t n, int64_t batch, af_stream stream) {
+af_status AFN(af_untangle_spectra)(af_layout layout, const rl* s_re, const rl* s_im, rl* a_re, rl* a_im, rl* b_re,
+                                   rl* b_im, int64_t n, int64_t batch, af_stream stream) {
   return AFN(af_untangle_spectra_2d)(layout, s_re, s_im, a_re, a_im, b_re, b_im, 1, n, batch, stream);
 }
 
-af_status AFN(af_cyclic_reverse_2d)(af_layout layout, const rl* in_re, const rl* in_im, rl* out_re,
-                               rl* out_im, int64_t height, int64_t width, int64_t batch, af_stream stream) {
+af_status AFN(af_cyclic_reverse_2d)(af_layout layout, const rl* in_re, const rl* in_im, rl* out_re, rl* out_im,
+                                    int64_t height, int64_t width, int64_t batch, af_stream stream) {
   AF_TRY
   if (height < 0 || width < 0 || batch < 0) return fail(AF_ERR_INVALID, "negative size");
   const i64 total = height * width * batch;
@@ -413,9 +411,8 @@ af_status AFN(af_cyclic_reverse_2d)(af_layout layout, const rl* in_re, const rl*
   AF_CATCH
 }
 
-af_status AFN(af_entangle_spectra)(af_layout layout, const rl* c_re, const rl* c_im, const rl* d_re,
-                              const rl* d_im, rl* out_re, rl* out_im, int64_t n, int64_t batch,
-                              af_stream stream) {
+af_status AFN(af_entangle_spectra)(af_layout layout, const rl* c_re, const rl* c_im, const rl* d_re, const rl* d_im,
+                                   rl* out_re, rl* out_im, int64_t n, int64_t batch, af_stream stream) {
   AF_TRY
   if (n < 0 || batch < 0) return fail(AF_ERR_INVALID, "negative size");
   if (n == 0 || batch == 0) return AF_OK;
@@ -451,15 +448,14 @@ static af_status two_to_impl(af_plan_s* const* plans, int dims, const rl* f, con
   AF_CATCH
 }
 
-af_status AFN(af_two_to_spectrum)(af_plan plan, const rl* f, const rl* g, af_layout layout, rl* a_re,
-                             rl* a_im, rl* b_re, rl* b_im, int64_t batch, af_stream stream) {
+af_status AFN(af_two_to_spectrum)(af_plan plan, const rl* f, const rl* g, af_layout layout, rl* a_re, rl* a_im,
+                                  rl* b_re, rl* b_im, int64_t batch, af_stream stream) {
   af_plan_s* plans[1] = {plan};
   return two_to_impl(plans, 1, f, g, layout, a_re, a_im, b_re, b_im, batch, stream);
 }
 
 af_status AFN(af_two_to_spectrum_2d)(af_plan plan0, af_plan plan1, const rl* f, const rl* g, af_layout layout,
-                                rl* a_re, rl* a_im, rl* b_re, rl* b_im, int64_t batch,
-                                af_stream stream) {
+                                     rl* a_re, rl* a_im, rl* b_re, rl* b_im, int64_t batch, af_stream stream) {
   af_plan_s* plans[2] = {plan0, plan1};
   return two_to_impl(plans, 2, f, g, layout, a_re, a_im, b_re, b_im, batch, stream);
 }
@@ -486,22 +482,21 @@ static af_status two_from_impl(af_plan_s* const* plans, int dims, af_layout layo
   AF_CATCH
 }
 
-af_status AFN(af_two_from_spectrum)(af_plan plan, af_layout layout, const rl* a_re, const rl* a_im,
-                               const rl* b_re, const rl* b_im, rl* f, rl* g, int64_t batch,
-                               af_stream stream) {
+af_status AFN(af_two_from_spectrum)(af_plan plan, af_layout layout, const rl* a_re, const rl* a_im, const rl* b_re,
+                                    const rl* b_im, rl* f, rl* g, int64_t batch, af_stream stream) {
   af_plan_s* plans[1] = {plan};
   return two_from_impl(plans, 1, layout, a_re, a_im, b_re, b_im, f, g, batch, stream);
 }
 
-af_status AFN(af_two_from_spectrum_2d)(af_plan plan0, af_plan plan1, af_layout layout, const rl* a_re,
-                                  const rl* a_im, const rl* b_re, const rl* b_im, rl* f, rl* g,
-                                  int64_t batch, af_stream stream) {
+af_status AFN(af_two_from_spectrum_2d)(af_plan plan0, af_plan plan1, af_layout layout, const rl* a_re, const rl* a_im,
+                                       const rl* b_re, const rl* b_im, rl* f, rl* g, int64_t batch,
+                                       af_stream stream) {
   af_plan_s* plans[2] = {plan0, plan1};
   return two_from_impl(plans, 2, layout, a_re, a_im, b_re, b_im, f, g, batch, stream);
 }
 
 af_status AFN(af_convolve_cyclic)(af_plan plan, af_layout layout, const rl* x_re, const rl* x_im, const rl* y_re,
-                             const rl* y_im, rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
+                                  const rl* y_im, rl* out_re, rl* out_im, int64_t batch, af_stream stream) {
   AF_TRY
   if (!plan) return fail(AF_ERR_INVALID, "null plan");
   if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
