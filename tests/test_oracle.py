@@ -8,6 +8,8 @@
    seeded examples with the reference's tolerance: |x - y| <= 1e-10 absolute
    per element (Fourier.hs:34-47), lengths 0..100 like QuickCheck's lists.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -52,30 +54,44 @@ def floor_5smooth(n):
 
 
 # ------------------------------------------------------------------ pins
+def reference_tables():
+    """Tables the reference documents in its source comments (fixture made by
+    tests/golden/make_reference_tables.py from the reference tree)."""
+    import json
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "reference_tables.json")) as f:
+        return json.load(f)
+
+
 def test_rader_permutation_of_7_matches_reference_comment():
-    """Planned.hs:632-643: generator 3, powers 1 3 2 6 4 5, inverse 1 3 2 5 6 4."""
-    assert O().multiplicative_generator(7) == 3
+    """Planned.hs:621-643: generator 3, powers 1 3 2 6 4 5, inverse 1 3 2 5 6 4."""
+    t = reference_tables()["rader7"]
+    assert O().multiplicative_generator(7) == t["generator"] == 3
     perm, rev, inv = O().rader_perms(7)
-    assert list(perm + 1) == [1, 3, 2, 6, 4, 5]
-    assert list(inv + 1) == [1, 3, 2, 5, 6, 4]
+    assert list(perm + 1) == t["powers"]
+    assert list(inv + 1) == t["inverse"]
     assert list(rev) == [perm[(-i) % 6] for i in range(6)]
 
 
 def test_rader_exponent_matrix_of_7_matches_reference_comment():
-    """Planned.hs:635-641: rows/columns permuted by powers of 3."""
-    table = [[0, 1, 3, 2, 6, 4, 5], [0, 3, 2, 6, 4, 5, 1], [0, 2, 6, 4, 5, 1, 3],
-             [0, 6, 4, 5, 1, 3, 2], [0, 4, 5, 1, 3, 2, 6], [0, 5, 1, 3, 2, 6, 4]]
+    """Planned.hs:621-643: the exponent matrix j*k mod 7, then rows and columns
+    permuted by powers of the generator."""
+    t = reference_tables()["rader7"]
+    assert t["exponent_matrix"] == [[j * k % 7 for k in range(7)] for j in range(7)]
     perm, _, _ = O().rader_perms(7)
-    g = perm + 1
-    for i in range(6):
-        row = [0] + [int(g[i] * g[j] % 7) for j in range(6)]
-        assert row == table[i]
+    order = [0] + [int(v) + 1 for v in perm]
+    assert t["permuted_matrix"] == [[order[a] * order[b] % 7 for b in range(7)] for a in range(7)]
 
 
 def test_small5_permutation_matches_reference_comment():
-    """Private.hs:185-203: powers of the generator 2 mod 5 are 1 2 4 3."""
+    """Private.hs:185-202: transform5's Rader permutation 0 1 2 4 3 (powers of
+    the generator 2 mod 5) and the permuted exponent matrix."""
+    t = reference_tables()["small5"]
+    assert t["exponent_matrix"] == [[j * k % 5 for k in range(5)] for j in range(5)]
     perm, _, _ = O().rader_perms(5)
-    assert [0] + list(perm + 1) == [0, 1, 2, 4, 3]
+    order = [0] + [int(v) + 1 for v in perm]
+    assert order == t["permutation"]
+    assert t["permuted_matrix"] == [[order[a] * order[b] % 5 for b in range(5)] for a in range(5)]
 
 
 def test_number_theory():
