@@ -17,6 +17,8 @@
 //   TILE_RADER      Rader's algorithm in one tile (Permutation.hs:24-80)
 //   TILE_BLUESTEIN  Bluestein in one tile (Private.hs:428-436)
 //   TILE_CONVROW    middle pass of a four-step cyclic convolution (Planned.hs:803-821)
+#include <atomic>
+
 #include "af_device.cuh"
 #include "af_internal.h"
 
@@ -712,8 +714,9 @@ size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
 // once per process (the opt-in limit less the kernel's static usage).
 template <int T, bool GEN>
 static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
-  static int limit = -1;
-  if (limit < 0) {
+  // set once per process; threads that race here compute and store the same value
+  static std::atomic<int> limit{-1};
+  if (limit.load(std::memory_order_acquire) < 0) {
     int dev = 0, optin = 0;
     cudaFuncAttributes fa;
     cudaError_t e = cudaGetDevice(&dev);
@@ -726,9 +729,9 @@ static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double*
       cudaGetLastError();
       return e;
     }
-    limit = optin - (int)fa.sharedSizeBytes;
+    limit.store(optin - (int)fa.sharedSizeBytes, std::memory_order_release);
   }
-  if (L.smem_bytes > (size_t)limit) return cudaErrorInvalidValue;
+  if (L.smem_bytes > (size_t)limit.load(std::memory_order_relaxed)) return cudaErrorInvalidValue;
   tile_kernel<T, GEN><<<L.nitems, T, L.smem_bytes, st>>>(L.descs, L.items, bases, loss, L.smem_data);
   return cudaGetLastError();
 }
