@@ -104,6 +104,10 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Starts sampling and returns once the first sample has arrived (at
+        most a few seconds), so that the samples taken after it fall inside
+        the timed region that follows."""
+        self.mark = 0
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -112,6 +116,11 @@ class ClockSampler:
             self.t.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while not self.lines and time.time() < deadline and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.mark = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -127,7 +136,10 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # the samples taken while the timed region ran; the last one before it
+        # when the region was shorter than the sampling interval
+        window = self.lines[self.mark:] or self.lines[-1:]
+        for ln in window:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -465,10 +477,12 @@ def run_reference(args):
         return
     ns = workload_sizes()
     vals = []
+    # each step is a bounded sample of the workload; the whole run stays
+    # near a minute of CPU time whatever --steps is
     for _ in range(args.warmup):
-        cpu_baseline(ns, budget_s=3.0)
+        cpu_baseline(ns, budget_s=min(3.0, 10.0 / max(args.warmup, 1)))
     for _ in range(args.steps):
-        v, cores, sample = cpu_baseline(ns, budget_s=6.0)
+        v, cores, sample = cpu_baseline(ns, budget_s=min(6.0, 60.0 / max(args.steps, 1)))
         vals.append(v)
     v = float(np.median(vals))
     out = {
@@ -488,7 +502,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
