@@ -194,7 +194,7 @@ struct TileDesc {
   int nlines;        // total lines of the step (all CTAs)
   int LS;            // shared-memory stride between lines (unpadded units)
   int slen;          // elements per line held in shared memory (M for conv tiles)
-  int tw_total;      // cx table entries staged in shared memory
+  int tw_total;      // table entries staged in shared memory
   int nph;
   const cx* tw_src;  // table source (device)
   FftPhase ph[AF_MAXPH];
@@ -239,7 +239,7 @@ struct WorkItem {
 };
 
 // ---------------------------------------------------------------- smem layout
-// One padding slot every 2^sh cx keeps strided Stockham accesses off bank
+// One padding slot every 2^sh elements keeps strided Stockham accesses off bank
 // conflicts; each tile picks sh (sh = 31: no padding).
 __device__ __forceinline__ int spd_(int i, int sh) { return i + (i >> sh); }
 
@@ -383,7 +383,7 @@ template <> struct Dft<5> {
 
 // Odd prime radix (7, 11, 13): symmetric direct DFT with the constants
 // cos(2 pi m/R), sin(2 pi m/R), m <= (R-1)/2 (computed in double precision
-// and rounded to rl).
+// and rounded to the element type).
 template <int R> struct OddRoots;
 template <> struct OddRoots<7> {
   static __device__ __forceinline__ rl c(int m) {
@@ -461,7 +461,7 @@ template <> struct Dft<13> : DftOdd<13> {};
 
 // Roots of unity for the composite radices: Roots<R>::c(m) = cos(2 pi m/R),
 // Roots<R>::s(m) = sin(2 pi m/R), m < R (computed in double precision and
-// rounded to rl).
+// rounded to the element type).
 template <int R> struct Roots;
 template <> struct Roots<6> {
   static __device__ __forceinline__ rl c(int m) {

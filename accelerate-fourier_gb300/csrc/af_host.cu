@@ -1620,7 +1620,7 @@ cudaError_t batch_run(BatchPlan* B, bool inverse, const cx* in, cx* out, const r
   const Program& prog = w ? B->cot : (inverse ? B->inv : B->fwd);
   TileBases bases = make_bases((const rl*)in, nullptr, (rl*)out, nullptr, B->ws, w, nullptr);
   if (w) {
-    // weights are real: BUF_AUX is read as a rl plane indexed like the output
+    // weights are real: BUF_AUX is read as a real plane indexed like the output
     bases.c[BUF_AUX] = nullptr;
     bases.re[BUF_AUX] = (rl*)w;
   }

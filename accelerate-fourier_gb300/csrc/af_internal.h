@@ -15,7 +15,7 @@ struct LaunchSpec {
   const WorkItem* items;
   int nitems;
   int threads;
-  int smem_data;      // cx per ping-pong buffer (max over the launch's descriptors)
+  int smem_data;      // elements per ping-pong buffer (max over the launch's descriptors)
   int generic;        // 0: every descriptor is a one-phase PLAIN tile with AFFINE views
   size_t smem_bytes;  // dynamic shared memory of the launch
 };

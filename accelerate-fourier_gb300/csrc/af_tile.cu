@@ -703,8 +703,8 @@ __global__ void __launch_bounds__(T, AF_MIN_CTAS(T)) tile_kernel(const TileDesc*
   tile_body<T, GEN>(*d, it, bases, A, Bf, tab, xs, loss);
 }
 
-// descriptor, two buffers, tables, per-line scratch (4 cx per line; at
-// least 8: the loss reduction keeps one rl per warp there)
+// descriptor, two buffers, tables, per-line scratch (4 elements per line; at
+// least 8: the loss reduction keeps one real per warp there)
 size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
   const int scratch = 4 * G > 8 ? 4 * G : 8;  // Rader x0/sum pairs, then the line bases
   return (sizeof(TileDesc) + 15) / 16 * 16 + (size_t)(2 * smem_data + tw_total + scratch) * sizeof(cx);
