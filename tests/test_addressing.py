@@ -122,3 +122,28 @@ def test_axis_addressing_f64(n):
     for outer, inner in [(1, 1), (1, 7), (3, 5), (2, 64)]:
         if n * outer * inner <= (1 << 22):
             check_axis(n, outer, inner, double=True)
+
+
+def describe_batch(sizes, double=False, which=0):
+    """Dry-run text of a batch program: one line per launch with its tiles."""
+    from accelerate_fourier import _lib
+    L = _lib.load()
+    f = L.afx_describe_batch_f64 if double else L.afx_describe_batch
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+    f.restype = ctypes.c_int
+    a = np.ascontiguousarray(np.asarray(sizes, dtype=np.int64))
+    buf = ctypes.create_string_buffer(1 << 16)
+    assert f(a.ctypes.data, len(a), -1, which, buf, len(buf)) == 0, buf.value.decode()
+    return buf.value.decode()
+
+
+def test_f64_tiles_hold_half_the_elements():
+    """A Complex Double tile holds at most 6200 elements (twice the shared
+    memory per element): 8192 and 7776 are single tiles in FP32 and four-step
+    transforms in FP64; 4096 is a single tile in both."""
+    f32, f64 = describe_batch([8192, 7776, 4096]), describe_batch([8192, 7776, 4096], double=True)
+    for n in (8192, 7776):
+        assert f"n{n} s{n} " in f32
+        assert f"n{n} s{n} " not in f64
+    assert "n4096 s4096 " in f32 and "n4096 s4096 " in f64
+    assert len(f64.strip().split("\n")) > len(f32.strip().split("\n"))
