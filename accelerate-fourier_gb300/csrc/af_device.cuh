@@ -64,8 +64,15 @@ __device__ __forceinline__ FastDiv make_fastdiv_dev(unsigned d) {
   f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
   return f;
 }
-__device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
-  return f.d <= 1 ? x : ((__umulhi(x, f.m) + x) >> f.s);
+AF_HD unsigned umulhi32(unsigned a, unsigned b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (unsigned)(((unsigned long long)a * b) >> 32);
+#endif
+}
+AF_HD unsigned fdiv(unsigned x, const FastDiv& f) {
+  return f.d <= 1 ? x : ((umulhi32(x, f.m) + x) >> f.s);
 }
 
 // (a * b) mod n for a, b < n < 2^31 without 64-bit division: rcp =
@@ -80,15 +87,22 @@ static inline ModN make_modn(unsigned long long n) {
   m.rcp = n ? (~0ull) / n : 0;
   return m;
 }
-__device__ __forceinline__ unsigned mod_of(unsigned long long x, const ModN& M) {
-  const unsigned long long q = __umul64hi(x, M.rcp);
+AF_HD unsigned long long umulhi64(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+AF_HD unsigned mod_of(unsigned long long x, const ModN& M) {
+  const unsigned long long q = umulhi64(x, M.rcp);
   unsigned long long r = x - q * M.n;
 #pragma unroll
   for (int k = 0; k < 2; ++k)
     if (r >= M.n) r -= M.n;
   return (unsigned)r;
 }
-__device__ __forceinline__ unsigned mulmod(unsigned a, unsigned b, const ModN& M) {
+AF_HD unsigned mulmod(unsigned a, unsigned b, const ModN& M) {
   return mod_of((unsigned long long)a * b, M);
 }
 
@@ -259,14 +273,14 @@ __device__ __forceinline__ cx tw_lookup(const cx* tab, int S_log2, int t, rl sig
 template <int R> struct Dft;
 
 template <> struct Dft<2> {
-  static __device__ __forceinline__ void run(cx* u, rl, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl, const cx*, int, int) {
     cx a = u[0], b = u[1];
     u[0] = cadd(a, b);
     u[1] = csub(a, b);
   }
 };
 
-__device__ __forceinline__ void dft4(cx& u0, cx& u1, cx& u2, cx& u3, rl sign) {
+AF_HD void dft4(cx& u0, cx& u1, cx& u2, cx& u3, rl sign) {
   cx t0 = cadd(u0, u2), t1 = csub(u0, u2);
   cx t2 = cadd(u1, u3), t3 = mul_si(csub(u1, u3), sign);
   u0 = cadd(t0, t2);
@@ -276,7 +290,7 @@ __device__ __forceinline__ void dft4(cx& u0, cx& u1, cx& u2, cx& u3, rl sign) {
 }
 
 template <> struct Dft<4> {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl sign, const cx*, int, int) {
     dft4(u[0], u[1], u[2], u[3], sign);
   }
 };
@@ -286,7 +300,7 @@ template <> struct Dft<4> {
 #define AF_S8 ((rl)0.38268343236508977173)
 
 // multiply by w8^m = exp(sign*2*pi*i*m/8)
-__device__ __forceinline__ cx mul_w8(cx a, int m, rl sign) {
+AF_HD cx mul_w8(cx a, int m, rl sign) {
   switch (m & 7) {
     case 0: return a;
     case 1: return cmul(a, make_cx(AF_R2, sign * AF_R2));
@@ -300,7 +314,7 @@ __device__ __forceinline__ cx mul_w8(cx a, int m, rl sign) {
 }
 
 template <> struct Dft<8> {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl sign, const cx*, int, int) {
     cx a[4], b[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -350,7 +364,7 @@ template <> struct Dft<16> {
 };
 
 template <> struct Dft<3> {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl sign, const cx*, int, int) {
     const rl c = (rl)-0.5, s = (rl)0.86602540378443864676 * sign;
     cx t = cadd(u[1], u[2]);
     cx d = csub(u[1], u[2]);
@@ -363,7 +377,7 @@ template <> struct Dft<3> {
 };
 
 template <> struct Dft<5> {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl sign, const cx*, int, int) {
     const rl c1 = (rl)0.30901699437494742410, c2 = (rl)-0.80901699437494742410;
     const rl s1 = (rl)0.95105651629515357212 * sign, s2 = (rl)0.58778525229247312917 * sign;
     cx p1 = cadd(u[1], u[4]), m1 = csub(u[1], u[4]);

@@ -1,0 +1,698 @@
+// af_fast.cu -- the batched executor of libaf: many Complex Float transforms
+// of mixed lengths run as work items of one kernel (af_fast.cuh).
+//
+// Each transform of the batch is either
+//   * direct: a 5-smooth length n, its mixed-radix FFT in one CTA
+//     (several transforms of one length may share a CTA), or for long n a
+//     four-step transform in two passes through an L2-resident workspace
+//     (Planned.hs:525-557: columns, twiddle, rows);
+//   * Bluestein: any other length, the chirp-z convolution of a 5-smooth
+//     length M >= 2n-1 (Planned.hs:744-773, transformChirp235), in one CTA or
+//     in three passes (columns, rows with the spectrum product, columns).
+// The same code runs on the host, one thread index at a time, in the
+// emulator that the CPU tests use.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "af_fast.cuh"
+#include "af_fast_host.h"
+
+namespace af {
+
+// ============================================================ table generation
+// Root tables hold forward roots W_den^num = exp(-2 pi i num / den), computed
+// in double precision from the exactly reduced exponent and rounded to float.
+AF_HD void root_segment_entry(const RootSeg& s, i64 i, i64* num, i64* den) {
+  if (s.kind == RS_STOCK) {  // Stockham pass: entry k*R + m = W_{pR}^(k m)
+    const i64 k = i / s.b, m = i % s.b;
+    *num = k * m;
+    *den = s.a * s.b;
+  } else {  // RS_LINEAR: entry i = W_a^(i * b)
+    *num = i * s.b;
+    *den = s.a;
+  }
+}
+
+AF_HD cx root_value(i64 num, i64 den) {
+  i64 r = num % den;
+  if (r < 0) r += den;
+  double c, s;
+#ifdef __CUDA_ARCH__
+  sincospi(-2.0 * (double)r / (double)den, &s, &c);
+#else
+  const double a = -2.0 * M_PI * ((double)r / (double)den);
+  s = std::sin(a);
+  c = std::cos(a);
+#endif
+  return make_cx((float)c, (float)s);
+}
+
+__global__ void root_tables_kernel(const RootSeg* segs, int nseg, cx* base) {
+  for (int si = blockIdx.x; si < nseg; si += gridDim.x) {
+    const RootSeg s = segs[si];
+    for (i64 i = threadIdx.x; i < s.count; i += blockDim.x) {
+      i64 num, den;
+      root_segment_entry(s, i, &num, &den);
+      base[s.off + i] = root_value(num, den);
+    }
+  }
+}
+
+void gen_root_tables(const std::vector<RootSeg>& segs, cx* dbase, cx* hbase, cudaStream_t st) {
+  if (segs.empty()) return;
+  if (hbase) {
+    for (const RootSeg& s : segs)
+      for (i64 i = 0; i < s.count; ++i) {
+        i64 num, den;
+        root_segment_entry(s, i, &num, &den);
+        hbase[s.off + i] = root_value(num, den);
+      }
+    return;
+  }
+  RootSeg* d = nullptr;
+  fcheck(cudaMallocAsync((void**)&d, sizeof(RootSeg) * segs.size(), st), "table segments");
+  fcheck(cudaMemcpyAsync(d, segs.data(), sizeof(RootSeg) * segs.size(), cudaMemcpyHostToDevice, st),
+         "table segments");
+  root_tables_kernel<<<(int)std::min<size_t>(segs.size(), 4096), 256, 0, st>>>(d, (int)segs.size(), dbase);
+  fcheck(cudaGetLastError(), "table kernel");
+  fcheck(cudaFreeAsync(d, st), "table segments");
+}
+
+// ============================================================ execution policies
+// Device: each phase is one call per thread followed by a barrier.
+struct DevExec {
+  double loc = 0.0;  // the thread's running sum over every item it ran
+#ifdef __CUDACC__
+  template <class F>
+  __device__ __forceinline__ void phase(F&& f) {
+    f((int)threadIdx.x);
+    __syncthreads();
+  }
+  template <class F>
+  __device__ __forceinline__ void phase_async(F&& f) {
+    f((int)threadIdx.x);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+  }
+  // a phase whose threads accumulate into their own running sum
+  template <class F>
+  __device__ __forceinline__ void phase_sum(F&& f) {
+    float l = 0.f;
+    f((int)threadIdx.x, l);
+    loc += l;
+    __syncthreads();
+  }
+  // block sum of every thread's local value, added to *acc (one atomic per CTA)
+  __device__ __forceinline__ void finish_sum(double* acc, double* red, int T) {
+    double v = loc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < T / 32; ++w) s += red[w];
+      atomicAdd(acc, s);
+    }
+  }
+#endif
+};
+
+// Host: each phase runs for every thread index in turn.
+struct HostExec {
+  int T;
+  std::vector<double> locs;
+  explicit HostExec(int t) : T(t), locs(t, 0.0) {}
+  template <class F>
+  void phase(F&& f) {
+    for (int t = 0; t < T; ++t) f(t);
+  }
+  template <class F>
+  void phase_async(F&& f) {
+    phase(f);
+  }
+  template <class F>
+  void phase_sum(F&& f) {
+    for (int t = 0; t < T; ++t) {
+      float l = 0.f;
+      f(t, l);
+      locs[t] += l;
+    }
+  }
+  void finish_sum(double* acc, double*, int) {
+    double s = 0;
+    for (double v : locs) s += v;
+    *acc += s;
+  }
+};
+
+AF_HD void cp_async8(cx* sdst, const cx* gsrc) {
+#ifdef __CUDA_ARCH__
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+#else
+  *sdst = *gsrc;
+#endif
+}
+// two elements; both addresses 16-byte aligned
+AF_HD void cp_async16(cx* sdst, const cx* gsrc) {
+#ifdef __CUDA_ARCH__
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+#else
+  sdst[0] = gsrc[0];
+  sdst[1] = gsrc[1];
+#endif
+}
+
+AF_HD int ilog2i(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
+// ============================================================ items
+// Output of a transform: plain store, or the cotangent epilogue g = 2 w X
+// with loss += w |X|^2 (w at the output's index).
+struct Sink {
+  cx* out;
+  const float* w;
+  AF_HD void put(i64 o, cx v, float& loss) const {
+    if (w) {
+      const float wt = ldf(w + o);
+      loss += wt * (v.x * v.x + v.y * v.y);
+      v = cscale(v, 2.f * wt);
+    }
+    out[o] = v;
+  }
+};
+
+// workspace element written by another CTA of this launch: read at L2 (no
+// stale L1 line)
+AF_HD cx ldws(const cx* p) {
+#ifdef __CUDA_ARCH__
+  return __ldcg(p);
+#else
+  return *p;
+#endif
+}
+
+// W_N^t from a two-level table: 256 low entries W_N^j, then W_N^(256 j)
+AF_HD cx tw2(const cx* tab, unsigned t) { return cmul(ldcx(tab + 256 + (t >> 8)), ldcx(tab + (t & 255u))); }
+// Bluestein chirp a_m = W_{2n}^(m^2 mod 2n) (forward root; the exact index
+// keeps the phase of large m accurate)
+AF_HD cx chirp_at(const FXform& x, int m) { return tw2(x.ct, mulmod((unsigned)m, (unsigned)m, x.mod2n)); }
+AF_HD cx conjc(cx a) { return make_cx(a.x, -a.y); }
+
+// The radix-G pass over `cnt` transforms of a full-FFT shape: element k1 of
+// line l of transform q at src[(q G + l) LS + k1].  Per unit the sink gives
+// a context c = f.at(q); f(c, q, m, v, loss) then receives natural bin
+// m = k1 + L*l'.
+template <int G, int SIGN, class F>
+AF_HD void final_unit(int q, int k1, int L1, const cx* src, int LS, const cx* ftw, F& f, float& loss) {
+  cx a[G];
+#pragma unroll
+  for (int l = 0; l < G; ++l) a[l] = src[lpos(k1, q * G + l, LS)];
+  final_radix<G, SIGN>(a, G > 1 ? ftw[k1] : make_cx(1.f, 0.f));
+  const auto c = f.at(q);
+#pragma unroll
+  for (int l = 0; l < G; ++l) f(c, q, k1 + l * L1, a[l], loss);
+}
+template <int G, int SIGN, class F>
+AF_HD void final_thread(int tid, int T, int cnt, const FShape& S, const cx* src, int LS, const cx* ftw, F& f,
+                        float& loss) {
+  const int L1 = S.line.L;
+  if (cnt == 1) {
+    for (int k1 = tid; k1 < L1; k1 += T) final_unit<G, SIGN>(0, k1, L1, src, LS, ftw, f, loss);
+    return;
+  }
+  for (int u = tid; u < cnt * L1; u += T) {
+    const int q = (int)fdiv((unsigned)u, S.L1div);
+    final_unit<G, SIGN>(q, u - q * L1, L1, src, LS, ftw, f, loss);
+  }
+}
+template <int SIGN, class F>
+AF_HD void final_any(int tid, int T, int cnt, const FShape& S, const cx* src, int LS, const cx* ftw, F& f,
+                     float& loss) {
+  switch (S.G) {
+    case 1: final_thread<1, SIGN>(tid, T, cnt, S, src, LS, ftw, f, loss); break;
+    case 2: final_thread<2, SIGN>(tid, T, cnt, S, src, LS, ftw, f, loss); break;
+    case 4: final_thread<4, SIGN>(tid, T, cnt, S, src, LS, ftw, f, loss); break;
+    default: final_thread<8, SIGN>(tid, T, cnt, S, src, LS, ftw, f, loss); break;
+  }
+}
+
+// Every Stockham pass of the shape's line FFT, ping-ponging between the two
+// buffers; returns the buffer holding the result (line-major, stride S.LS).
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
+  const int np = S.line.npass;
+  for (int j = 0; j < np; ++j) {
+    const FPass& ps = S.line.pass[j];
+    const int LSo = j == np - 1 ? S.LS : 0;
+    ex.phase([&](int tid) {
+      if (S.V == 2) fpass_any<2, SIGN>(tid, T, src, dst, ps, S.GL, S.glog, LSo, tw);
+      else fpass_any<1, SIGN>(tid, T, src, dst, ps, S.GL, S.glog, LSo, tw);
+    });
+    cx* t = src;
+    src = dst;
+    dst = t;
+  }
+  return src;
+}
+
+// shared-memory areas of an item
+struct FSmem {
+  cx *a, *b, *tw, *ftw;
+  float* red;
+};
+AF_HD FSmem smem_of(const FShape& S, cx* sm) {
+  FSmem m;
+  m.a = sm;
+  m.b = sm + S.cap;
+  m.tw = m.b + S.cap;
+  m.ftw = m.tw + S.line.twn;
+  m.red = reinterpret_cast<float*>(m.ftw + S.ftwn);
+  return m;
+}
+
+// copies the shape's tables (issued with the item's asynchronous loads)
+AF_HD void copy_tables(int tid, int T, const FShape& S, const FSmem& m) {
+  for (int i = tid; i < S.line.twn; i += T) cp_async8(m.tw + i, S.tw + i);
+  for (int i = tid; i < S.ftwn; i += T) cp_async8(m.ftw + i, S.ftw + i);
+}
+
+// n contiguous elements into shared memory: 16-byte copies when the source
+// is 16-byte aligned, else 8-byte copies
+AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
+  if ((reinterpret_cast<unsigned long long>(src) & 15) == 0) {
+    for (int i = 2 * tid; i + 1 < n; i += 2 * T) cp_async16(dst + i, src + i);
+    if ((n & 1) && tid == 0) cp_async8(dst + n - 1, src + n - 1);
+  } else {
+    for (int i = tid; i < n; i += T) cp_async8(dst + i, src + i);
+  }
+}
+
+// sink of the direct items: bin m of transform q to the output
+struct DirectOut {
+  Sink sk;
+  const FXform* xf;
+  AF_HD i64 at(int q) const { return xf[q].off; }
+  AF_HD void operator()(i64 base, int, int m, cx v, float& loss) const { sk.put(base + m, v, loss); }
+};
+
+// FK_DIRECT: Q transforms of one 5-smooth length, loaded in natural order
+// (G interleaved lines each), line FFT, radix-G pass to the output.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const int n = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
+  const FXform* xf = A.xf + it.first;
+  const int cnt = it.count;
+  ex.phase_async([&](int tid) {
+    if (Q == 1) {  // one transform: its natural order is the layout
+      load_contiguous(tid, T, m.a, A.in + xf[0].off, n);
+    } else {
+      for (int i = tid; i < Q * n; i += T) {
+        const int q = (int)fdiv((unsigned)i, S.ndiv);
+        const int e = i - q * n;
+        const int pos = ipos(e >> glogG, q * G + (e & (G - 1)), GL);
+        if (q < cnt) cp_async8(m.a + pos, A.in + xf[q].off + e);
+        else m.a[pos] = make_cx(0.f, 0.f);
+      }
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const int LS = S.line.npass ? S.LS : 1;  // no pass: the load layout read as line-major with LS 1
+  DirectOut f{Sink{A.out, A.w}, xf};
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, f, loss); });
+}
+
+// sinks of the Bluestein item: the spectrum product (conjugated) into the
+// other buffer, in the layout of the second FFT's input; and the chirp
+// product of the first n bins to the output
+struct BlueMid {
+  const FXform* xf;
+  int cnt;
+  cx* nxt;
+  int glogG, G, GL;
+  AF_HD const cx* at(int q) const { return q < cnt ? xf[q].spec : nullptr; }
+  template <int SIGN>
+  AF_HD void put(const cx* spec, int q, int m, cx v) const {
+    const cx p = spec ? conjc(cmul_s<SIGN>(v, ldcx(spec + m))) : make_cx(0.f, 0.f);
+    nxt[ipos(m >> glogG, q * G + (m & (G - 1)), GL)] = p;
+  }
+};
+template <int SIGN>
+struct BlueMidS : BlueMid {
+  AF_HD void operator()(const cx* spec, int q, int m, cx v, float&) const { put<SIGN>(spec, q, m, v); }
+};
+template <int SIGN>
+struct BlueOut {
+  Sink sk;
+  const FXform* xf;
+  AF_HD const FXform* at(int q) const { return xf + q; }
+  AF_HD void operator()(const FXform* x, int, int m, cx v, float& loss) const {
+    if (m < x->n) sk.put(x->off + m, cmul_s<SIGN>(conjc(v), chirp_at(*x, m)), loss);
+  }
+};
+
+// FK_BLUE: Bluestein in one CTA (Planned.hs:760-773): u = a (.) x zero padded
+// to M, FFT, times the spectrum, conjugate, FFT (= conj of the opposite-sign
+// FFT), y = a (.) conj(.) for the first n bins.  Q transforms sharing M.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const int M = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
+  const FXform* xf = A.xf + it.first;
+  const int cnt = it.count;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < Q * M; i += T) {
+      const int q = (int)fdiv((unsigned)i, S.ndiv);
+      const int e = i - q * M;
+      cx v = make_cx(0.f, 0.f);
+      if (q < cnt && e < xf[q].n) v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at(xf[q], e));
+      m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const int LS = S.line.npass ? S.LS : 1;
+  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* nxt = res == m.a ? m.b : m.a;
+  BlueMidS<SIGN> mid;
+  mid.xf = xf;
+  mid.cnt = cnt;
+  mid.nxt = nxt;
+  mid.glogG = glogG;
+  mid.G = G;
+  mid.GL = GL;
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, Q, S, res, LS, m.ftw, mid, loss); });
+  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  BlueOut<SIGN> out{Sink{A.out, A.w}, xf};
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, out, loss); });
+}
+
+// Multi-pass items work on one transform: columns [c0, c0 + cn) or lines
+// [c0, c0 + cn) of its n1 x n2 matrix (element (j1, j2) at j1 n2 + j2); the
+// shape's line FFT has GL lines (a power of two, cn <= GL).
+//
+// FK_COLS (four-step pass A, Planned.hs:525-557) and FK_BCOLS (Bluestein
+// pass A): column FFT_n1 of x (FK_BCOLS: of a (.) x zero padded), twiddle
+// W_N^(j2 k1), stored column-contiguous: ws[j2 n1 + k1].
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, cx* sm, bool blue) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = A.xf[it.first];
+  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int n2 = x.n2, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < L * GL; i += T) {
+      const int e = i >> glogC, c = i & (GL - 1);
+      const int j = e * n2 + c0 + c;  // natural index of element e of column c0 + c
+      if (c >= cn) m.a[i] = make_cx(0.f, 0.f);
+      else if (!blue) cp_async8(m.a + i, A.in + x.off + j);
+      else m.a[i] = j < x.n ? cmul_s<SIGN>(ldcx(A.in + x.off + j), chirp_at(x, j)) : make_cx(0.f, 0.f);
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  ex.phase([&](int tid) {
+    for (int u = tid; u < cn * L; u += T) {
+      const int c = (int)fdiv((unsigned)u, S.L1div);
+      const int k1 = u - c * L;
+      const int j2 = c0 + c;
+      const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tw2(x.wt, (unsigned)(j2 * k1)));
+      A.ws[x.ws + (i64)j2 * L + k1] = v;
+    }
+  });
+}
+
+// FK_ROWS (four-step pass B): lines k1 in [c0, c0 + cn), element j2 at
+// ws[j2 n1 + k1]; FFT_n2; X[k1 + n1 k2] to the output.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = A.xf[it.first];
+  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int n1 = x.n1, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < L * GL; i += T) {
+      const int e = i >> glogR, l = i & (GL - 1);
+      m.a[i] = l < cn ? ldws(A.ws + x.ws + (i64)e * n1 + c0 + l) : make_cx(0.f, 0.f);
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const Sink sk{A.out, A.w};
+  ex.phase_sum([&](int tid, float& loss) {
+    for (int u = tid; u < L * GL; u += T) {
+      const int k2 = u >> glogR, l = u & (GL - 1);
+      if (l < cn) sk.put(x.off + c0 + l + (i64)n1 * k2, res[lpos(k2, l, S.LS)], loss);
+    }
+  });
+}
+
+// FK_BROWS (Bluestein pass R): lines k1 in [c0, c0 + cn), element j2 at
+// ws[j2 M1 + k1]; FFT_M2; times the spectrum at k1 + M1 k2 and conjugated;
+// FFT_M2 again; twiddle W_M^(j2 k1); stored line-contiguous in the
+// transform's second workspace region: ws[M + k1 M2 + j2] (other items of
+// this pass still read the first).
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = A.xf[it.first];
+  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int M1 = x.n1, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < L * GL; i += T) {
+      const int e = i >> glogR, l = i & (GL - 1);
+      m.a[i] = l < cn ? ldws(A.ws + x.ws + (i64)e * M1 + c0 + l) : make_cx(0.f, 0.f);
+    }
+    copy_tables(tid, T, S, m);
+  });
+  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* nxt = res == m.a ? m.b : m.a;
+  ex.phase([&](int tid) {
+    for (int u = tid; u < L * GL; u += T) {
+      const int k2 = u >> glogR, l = u & (GL - 1);
+      cx p = make_cx(0.f, 0.f);
+      if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], ldcx(x.spec + c0 + l + (i64)M1 * k2)));
+      nxt[ipos(k2, l, GL)] = p;
+    }
+  });
+  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  ex.phase([&](int tid) {
+    for (int u = tid; u < cn * L; u += T) {
+      const int l = (int)fdiv((unsigned)u, S.L1div);
+      const int j2 = u - l * L;
+      const int k1 = c0 + l;
+      A.ws[x.ws + x.M + (i64)k1 * L + j2] = cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tw2(x.wt, (unsigned)(j2 * k1)));
+    }
+  });
+}
+
+// FK_BCOLS2 (Bluestein pass A'): columns j2 in [c0, c0 + cn), element k1 at
+// ws[M + k1 M2 + j2]; FFT_M1; y_m = a_m (.) conj(.) at m = j1 M2 + j2 < n.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  const FShape& S = A.shapes[it.shape];
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = A.xf[it.first];
+  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int M2 = x.n2, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < L * GL; i += T) {
+      const int e = i >> glogC, c = i & (GL - 1);
+      m.a[i] = c < cn ? ldws(A.ws + x.ws + x.M + (i64)e * M2 + c0 + c) : make_cx(0.f, 0.f);
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const Sink sk{A.out, A.w};
+  ex.phase_sum([&](int tid, float& loss) {
+    for (int u = tid; u < L * GL; u += T) {
+      const int j1 = u >> glogC, c = u & (GL - 1);
+      const int j = j1 * M2 + c0 + c;
+      if (c < cn && j < x.n) sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at(x, j)), loss);
+    }
+  });
+}
+
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void run_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+  switch (it.kind) {
+    case FK_BLUE: blue_item<T, SIGN>(ex, A, it, sm); break;
+    case FK_COLS: cols_item<T, SIGN>(ex, A, it, sm, false); break;
+    case FK_BCOLS: cols_item<T, SIGN>(ex, A, it, sm, true); break;
+    case FK_ROWS: rows_item<T, SIGN>(ex, A, it, sm); break;
+    case FK_BROWS: brows_item<T, SIGN>(ex, A, it, sm); break;
+    case FK_BCOLS2: bcols2_item<T, SIGN>(ex, A, it, sm); break;
+    default: direct_item<T, SIGN>(ex, A, it, sm); break;
+  }
+}
+
+// CTAs per SM the register budget allows for: 6 x 128, 3 x 256, 1 x 512 threads
+#define AFF_MINB(T) ((T) <= 128 ? 6 : ((T) <= 256 ? 3 : 1))
+
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+#endif
+
+// Persistent executor: every CTA takes the next item of the queue (items
+// wait only for items earlier in the queue, which CTAs already hold, so the
+// launch always completes).  A wait polls its counter at most spin_limit
+// times; then the CTA records FE_TIMEOUT and leaves, and the items that
+// depend on it time out in turn.
+template <int T, int SIGN>
+__global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitems, unsigned* ctrs,
+                                                              long long spin_limit) {
+  extern __shared__ float4 fsm4[];
+  __shared__ int s_item, s_ok;
+  DevExec ex;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int i = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+      int ok = 1;
+      if (i < nitems) {
+        const FItem it = A.items[i];
+        if (it.wait_ctr >= 0) {
+          long long k = 0;
+          while (ld_acquire(ctrs + it.wait_ctr) < (unsigned)it.wait_cnt) {
+            if (++k > spin_limit) {
+              atomicExch(ctrs + FC_ERROR, (unsigned)FE_TIMEOUT);
+              ok = 0;
+              break;
+            }
+            __nanosleep(64);
+          }
+        }
+      }
+      s_item = i;
+      s_ok = ok;
+    }
+    __syncthreads();
+    const int i = s_item;
+    if (i >= nitems || !s_ok) break;
+    const FItem it = A.items[i];
+    run_item<T, SIGN>(ex, A, it, reinterpret_cast<cx*>(fsm4));
+    // publish this item's global stores before counting it done
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && it.done_ctr >= 0) atomicAdd(ctrs + it.done_ctr, 1u);
+  }
+  if (A.w && A.loss) {
+    __syncthreads();
+    ex.finish_sum(A.loss, reinterpret_cast<double*>(fsm4), T);
+  }
+}
+
+template <int T, int SIGN>
+static cudaError_t launch_fast_t(const FArgs& A, int nitems, size_t smem, unsigned* ctrs, int grid,
+                                 long long spin_limit, cudaStream_t st) {
+  static std::mutex mu;
+  static int set_dev[64];
+  static bool init = false;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (!init) {
+      for (int& v : set_dev) v = -1;
+      init = true;
+    }
+    if (dev >= 64 || set_dev[dev] < (int)smem) {
+      e = cudaFuncSetAttribute(fast_kernel<T, SIGN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fast_kernel<T, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+      if (dev < 64) set_dev[dev] = (int)smem;
+    }
+  }
+  fast_kernel<T, SIGN><<<grid, T, smem, st>>>(A, nitems, ctrs, spin_limit);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fast(int T, int sign, const FArgs& A, int nitems, size_t smem, unsigned* ctrs, int grid,
+                        long long spin_limit, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  if (T != 256) return cudaErrorInvalidValue;
+  return sign < 0 ? launch_fast_t<256, -1>(A, nitems, smem, ctrs, grid, spin_limit, st)
+                  : launch_fast_t<256, 1>(A, nitems, smem, ctrs, grid, spin_limit, st);
+}
+
+int fast_ctas_per_sm(int T, int sign, size_t smem) {
+  int nb = 0;
+  if (T != 256) return 0;
+  cudaError_t e;
+  if (sign < 0) {
+    e = cudaFuncSetAttribute(fast_kernel<256, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(fast_kernel<256, -1>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_kernel<256, -1>, 256, smem);
+  } else {
+    e = cudaFuncSetAttribute(fast_kernel<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(fast_kernel<256, 1>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_kernel<256, 1>, 256, smem);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nb;
+}
+
+template <int T, int SIGN>
+static int emulate_t(const FArgs& A, const FItem* items, int nitems, size_t smem, int nctrs) {
+  std::vector<unsigned> ctr(std::max(nctrs, (int)FC_FIRST), 0u);
+  HostExec ex(T);
+  for (int i = 0; i < nitems; ++i) {
+    const FItem& it = items[i];
+    if (it.wait_ctr >= 0 && ctr.at(it.wait_ctr) < (unsigned)it.wait_cnt) return FE_TIMEOUT;
+    // exactly the shape's shared memory, so that the sanitizer sees overruns
+    const size_t bytes = (size_t)A.shapes[it.shape].smem;
+    if (bytes > smem) throw FastError("item needs more shared memory than its launch");
+    std::vector<cx> sm((bytes + sizeof(cx) - 1) / sizeof(cx));
+    run_item<T, SIGN>(ex, A, it, sm.data());
+    if (it.done_ctr >= 0) ctr.at(it.done_ctr)++;
+  }
+  if (A.w && A.loss) ex.finish_sum(A.loss, nullptr, T);
+  return FE_OK;
+}
+
+int emulate_fast(int T, int sign, const FArgs& A, const FItem* items, int nitems, size_t smem, int nctrs) {
+  if (T != 256) throw FastError("the executor runs 256-thread CTAs");
+  return sign < 0 ? emulate_t<256, -1>(A, items, nitems, smem, nctrs)
+                  : emulate_t<256, 1>(A, items, nitems, smem, nctrs);
+}
+
+}  // namespace af

@@ -1,0 +1,202 @@
+// af_fast.cuh -- the line-FFT engine of the batched executor (Complex Float).
+//
+// The building block is an FFT of length L over GL interleaved lines held in
+// shared memory: element e of line l sits at e*GL + l.  A transform of
+// length n = L*G is G such lines of its own natural order (x[e*G + l]), so a
+// contiguous copy of x already has this layout; a CTA may hold Q transforms
+// of one length (GL = Q*G lines).  Each Stockham pass (compile-time radix R)
+// reads R elements of a pair of adjacent lines as 16-byte vectors, applies
+// the pass twiddles W_{pR}^{k m} from a table in shared memory (one table
+// serves both lines) and the radix-R DFT of each line, and writes the pair
+// back.  The last pass writes line-major (line l at l*LS, LS odd), which both
+// epilogues read without bank conflicts: along a line (consecutive elements)
+// or across lines (stride LS).  A full transform ends with the radix-G pass
+// across the G lines (twiddle W_n^(l k1), DFT_G), whose outputs are the
+// natural-order spectrum X[k1 + L*l'].
+//
+// Everything below is __host__ __device__: the kernels run each phase once
+// per thread with a barrier after it, and the host emulator (used by the CPU
+// tests, with address sanitizer) runs the same phase for every thread index
+// in turn.  The algorithm is the mixed-radix Cooley-Tukey FFT that the
+// reference's split-radix and composite transforms compute
+// (src/Data/Array/Accelerate/Fourier/Planned.hs:473-557); the Bluestein
+// convolution follows Planned.hs:744-773.
+#pragma once
+#include "af_device.cuh"
+
+namespace af {
+
+#define AFF_MAXPASS 12
+
+// One Stockham pass of a line FFT: butterfly b reads elements b + m*nb and
+// writes q*p*R + k + m*p (k = b mod p, q = b div p) after the twiddles
+// W_{pR}^(k m), read from tw + k*R + m.
+struct FPass {
+  int R, p, nb, tw;
+  int plog;  // log2 p when p is a power of two, else -1
+  FastDiv pdiv;
+};
+struct FLine {
+  int L, npass, twn;  // length, passes, table entries
+  FPass pass[AFF_MAXPASS];
+};
+
+// shared-memory element positions of the two layouts
+AF_HD int ipos(int e, int line, int GL) { return e * GL + line; }
+AF_HD int lpos(int e, int line, int LS) { return line * LS + e; }
+// line-major stride: odd, so that a warp reading across lines hits distinct banks
+AF_HD int line_stride(int L) { return L | 1; }
+
+AF_HD cx ldcx(const cx* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+AF_HD float ldf(const float* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+
+// a * w (SIGN = -1) or a * conj(w) (SIGN = +1): tables hold forward roots
+template <int SIGN>
+AF_HD cx cmul_s(cx a, cx w) {
+  if (SIGN < 0) return cmul(a, w);
+  return make_cx(rfma(a.x, w.x, a.y * w.y), rfma(a.y, w.x, -a.x * w.y));
+}
+
+template <int V> struct FVec;
+template <> struct FVec<1> {
+  typedef float2 T;
+  static AF_HD void get(const cx* p, cx* a) { a[0] = *p; }
+  static AF_HD void put(cx* p, const cx* a) { *p = a[0]; }
+};
+template <> struct FVec<2> {
+  typedef float4 T;
+  static AF_HD void get(const cx* p, cx* a) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a[0] = make_cx(v.x, v.y);
+    a[1] = make_cx(v.z, v.w);
+  }
+  static AF_HD void put(cx* p, const cx* a) {
+    *reinterpret_cast<float4*>(p) = make_float4(a[0].x, a[0].y, a[1].x, a[1].y);
+  }
+};
+
+// Pass twiddles of butterfly k: w[m] = W_{pR}^(k m), m = 1..R-1
+template <int R>
+AF_HD void pass_twiddles(const cx* t, cx* w) {
+  if constexpr (R % 2 == 0) {
+#pragma unroll
+    for (int m = 0; m < R; m += 2) {
+      const float4 v = *reinterpret_cast<const float4*>(t + m);
+      if (m > 0) w[m] = make_cx(v.x, v.y);
+      w[m + 1] = make_cx(v.z, v.w);
+    }
+  } else {
+#pragma unroll
+    for (int m = 1; m < R; ++m) w[m] = t[m];
+  }
+}
+
+// One unit of a Stockham pass: butterfly b of the V lines starting at `line`.
+// LS == 0: interleaved output (GL lines); else line-major output with stride LS.
+template <int R, int V, int SIGN>
+AF_HD void fpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, const FPass& ps, int b, int line, int GL,
+                      int LS, const cx* __restrict__ tw) {
+  cx a[V][R];
+  const int ib = ipos(b, line, GL);
+  const int istep = ps.nb * GL;
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    cx t[V];
+    FVec<V>::get(src + ib + m * istep, t);
+#pragma unroll
+    for (int v = 0; v < V; ++v) a[v][m] = t[v];
+  }
+  const int q = ps.plog >= 0 ? b >> ps.plog : (int)fdiv((unsigned)b, ps.pdiv);
+  const int k = b - q * ps.p;
+  if (k > 0) {
+    cx w[R];
+    pass_twiddles<R>(tw + ps.tw + k * R, w);
+#pragma unroll
+    for (int m = 1; m < R; ++m)
+#pragma unroll
+      for (int v = 0; v < V; ++v) a[v][m] = cmul_s<SIGN>(a[v][m], w[m]);
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) Dft<R>::run(a[v], (rl)SIGN, nullptr, 0, 0);
+  const int oe = q * ps.p * R + k;
+  if (LS == 0) {
+    const int ob = ipos(oe, line, GL);
+    const int ostep = ps.p * GL;
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      cx t[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) t[v] = a[v][m];
+      FVec<V>::put(dst + ob + m * ostep, t);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int m = 0; m < R; ++m) dst[lpos(oe + m * ps.p, line + v, LS)] = a[v][m];
+  }
+}
+
+// All units of one pass for thread `tid` of T (GL lines, V lines per unit).
+template <int R, int V, int SIGN>
+AF_HD void fpass_thread(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int glog, int LS,
+                        const cx* tw) {
+  const int units = ps.nb << glog;
+  const int gmask = (1 << glog) - 1;
+  for (int u = tid; u < units; u += T) {
+    const int b = u >> glog;
+    const int line = (u & gmask) * V;
+    fpass_unit<R, V, SIGN>(src, dst, ps, b, line, GL, LS, tw);
+  }
+}
+
+template <int V, int SIGN>
+AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int glog, int LS,
+                     const cx* tw) {
+  switch (ps.R) {
+    case 2: fpass_thread<2, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    case 3: fpass_thread<3, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    case 4: fpass_thread<4, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    case 5: fpass_thread<5, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    default: fpass_thread<8, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+  }
+}
+
+// w^l for l < G from w (at most three products deep for G <= 16)
+template <int G>
+AF_HD void powers(cx w, cx* p) {
+  p[0] = make_cx(1.f, 0.f);
+  if (G > 1) p[1] = w;
+#pragma unroll
+  for (int l = 2; l < G; ++l) {
+    const int h = l / 2;
+    p[l] = cmul(p[h], p[l - h]);
+  }
+}
+
+// The radix-G pass across the G lines of one transform: inputs a[l] =
+// element k1 of line l; outputs natural-order bins k1 + L1*l'.
+template <int G, int SIGN>
+AF_HD void final_radix(cx* a, cx w) {
+  if constexpr (G > 1) {
+    cx p[G];
+    powers<G>(w, p);
+#pragma unroll
+    for (int l = 1; l < G; ++l) a[l] = cmul_s<SIGN>(a[l], p[l]);
+    Dft<G>::run(a, (rl)SIGN, nullptr, 0, 0);
+  }
+}
+
+}  // namespace af
