@@ -29,8 +29,8 @@ namespace af {
 // Root tables hold forward roots W_den^num = exp(-2 pi i num / den), computed
 // in double precision from the exactly reduced exponent and rounded to float.
 AF_HD void root_segment_entry(const RootSeg& s, i64 i, i64* num, i64* den) {
-  if (s.kind == RS_STOCK) {  // Stockham pass: entry k*R + m = W_{pR}^(k m)
-    const i64 k = i / s.b, m = i % s.b;
+  if (s.kind == RS_STOCK) {  // Stockham pass: entry (m-1)*p + k = W_{pR}^(k m)
+    const i64 k = i % s.a, m = i / s.a + 1;
     *num = k * m;
     *den = s.a * s.b;
   } else {  // RS_LINEAR: entry i = W_a^(i * b)
@@ -204,11 +204,32 @@ AF_HD cx ldws(const cx* p) {
 #endif
 }
 
-// W_N^t from a two-level table: 256 low entries W_N^j, then W_N^(256 j)
-AF_HD cx tw2(const cx* tab, unsigned t) { return cmul(ldcx(tab + 256 + (t >> 8)), ldcx(tab + (t & 255u))); }
+// W_N^t, t < 2^18, from a three-level table of 3 x 64 entries: W_N^j,
+// W_N^(64 j), W_N^(4096 j).  GLOBAL: the table is in global memory (read
+// through the read-only path), else in shared memory.
+template <bool GLOBAL>
+AF_HD cx tl3(const cx* tab, unsigned t) {
+  cx a, b, c;
+  if (GLOBAL) {
+    a = ldcx(tab + (t & 63u));
+    b = ldcx(tab + 64 + ((t >> 6) & 63u));
+    c = ldcx(tab + 128 + (t >> 12));
+  } else {
+    a = tab[t & 63u];
+    b = tab[64 + ((t >> 6) & 63u)];
+    c = tab[128 + (t >> 12)];
+  }
+  return cmul(cmul(c, b), a);
+}
 // Bluestein chirp a_m = W_{2n}^(m^2 mod 2n) (forward root; the exact index
-// keeps the phase of large m accurate)
-AF_HD cx chirp_at(const FXform& x, int m) { return tw2(x.ct, mulmod((unsigned)m, (unsigned)m, x.mod2n)); }
+// keeps the phase of large m accurate); ct is the three-level table of W_{2n}
+template <bool GLOBAL>
+AF_HD cx chirp_at(const FXform& x, const cx* ct, int m) {
+  return tl3<GLOBAL>(ct, mulmod((unsigned)m, (unsigned)m, x.mod2n));
+}
+// Bluestein spectrum entry k of M: the spectrum of the even chirp is even,
+// so only entries 0..M/2 are stored
+AF_HD cx spec_at(const cx* spec, int M, int k) { return ldcx(spec + (2 * k <= M ? k : M - k)); }
 AF_HD cx conjc(cx a) { return make_cx(a.x, -a.y); }
 
 // The radix-G pass over `cnt` transforms of a full-FFT shape: element k1 of
@@ -256,7 +277,7 @@ template <int T, int SIGN, class E>
 AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
   const int np = S.line.npass;
   for (int j = 0; j < np; ++j) {
-    const FPass& ps = S.line.pass[j];
+    const FPass ps = S.line.pass[j];
     const int LSo = j == np - 1 ? S.LS : 0;
     ex.phase([&](int tid) {
       if (S.V == 2) fpass_any<2, SIGN>(tid, T, src, dst, ps, S.GL, S.glog, LSo, tw);
@@ -269,9 +290,11 @@ AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
   return src;
 }
 
-// shared-memory areas of an item
+// shared-memory areas of an item: the two data buffers, the pass twiddles,
+// the final twiddles, the staged three-level tables (multi-pass shapes), and
+// the reduction scratch
 struct FSmem {
-  cx *a, *b, *tw, *ftw;
+  cx *a, *b, *tw, *ftw, *wt3, *ct3;
   float* red;
 };
 AF_HD FSmem smem_of(const FShape& S, cx* sm) {
@@ -280,14 +303,20 @@ AF_HD FSmem smem_of(const FShape& S, cx* sm) {
   m.b = sm + S.cap;
   m.tw = m.b + S.cap;
   m.ftw = m.tw + S.line.twn;
-  m.red = reinterpret_cast<float*>(m.ftw + S.ftwn);
+  m.wt3 = m.ftw + S.ftwn;
+  m.ct3 = m.wt3 + (S.aux ? AFF_TL3 : 0);
+  m.red = reinterpret_cast<float*>(m.ct3 + (S.aux ? AFF_TL3 : 0));
   return m;
 }
 
-// copies the shape's tables (issued with the item's asynchronous loads)
+// copies the shape's tables (issued with the item's asynchronous loads);
+// every table starts on an even entry, so 16-byte copies
+AF_HD void copy_table(int tid, int T, cx* dst, const cx* src, int n) {
+  for (int i = 2 * tid; i < n; i += 2 * T) cp_async16(dst + i, src + i);
+}
 AF_HD void copy_tables(int tid, int T, const FShape& S, const FSmem& m) {
-  for (int i = tid; i < S.line.twn; i += T) cp_async8(m.tw + i, S.tw + i);
-  for (int i = tid; i < S.ftwn; i += T) cp_async8(m.ftw + i, S.ftw + i);
+  copy_table(tid, T, m.tw, S.tw, S.line.twn);
+  copy_table(tid, T, m.ftw, S.ftw, S.ftwn);
 }
 
 // n contiguous elements into shared memory: 16-byte copies when the source
@@ -298,6 +327,37 @@ AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
     if ((n & 1) && tid == 0) cp_async8(dst + n - 1, src + n - 1);
   } else {
     for (int i = tid; i < n; i += T) cp_async8(dst + i, src + i);
+  }
+}
+
+// Lines [0, cn) of a strided matrix, rows e < L, into the interleaved layout
+// dst[e GL + c] = src[e stride + c] (lines cn..GL-1 zero).  Pairs of lines move
+// as 16-byte copies at L2 when every pair is 16-byte aligned; otherwise one
+// element at a time, at L2 for workspace sources (WS: written by other CTAs
+// of this launch, so never read through L1).
+template <bool WS>
+AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn) {
+  const bool v16 = GL >= 2 && ((reinterpret_cast<unsigned long long>(src) & 15) == 0) && (stride % 2 == 0) &&
+                   (cn % 2 == 0);
+  if (v16) {
+    const int hlog = glog - 1, half = GL >> 1;
+    for (int i = tid; i < L * half; i += T) {
+      const int e = i >> hlog, c = (i & (half - 1)) * 2;
+      cx* d = dst + e * GL + c;
+      if (c < cn) {
+        cp_async16(d, src + e * stride + c);
+      } else {
+        d[0] = make_cx(0.f, 0.f);
+        d[1] = make_cx(0.f, 0.f);
+      }
+    }
+  } else {
+    for (int i = tid; i < L * GL; i += T) {
+      const int e = i >> glog, c = i & (GL - 1);
+      if (c >= cn) dst[i] = make_cx(0.f, 0.f);
+      else if (WS) dst[i] = ldws(src + e * stride + c);
+      else cp_async8(dst + i, src + e * stride + c);
+    }
   }
 }
 
@@ -313,11 +373,9 @@ struct DirectOut {
 // (G interleaved lines each), line FFT, radix-G pass to the output.
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
   const int n = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
-  const FXform* xf = A.xf + it.first;
   const int cnt = it.count;
   ex.phase_async([&](int tid) {
     if (Q == 1) {  // one transform: its natural order is the layout
@@ -344,13 +402,13 @@ AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
 // product of the first n bins to the output
 struct BlueMid {
   const FXform* xf;
-  int cnt;
+  int cnt, M;
   cx* nxt;
   int glogG, G, GL;
   AF_HD const cx* at(int q) const { return q < cnt ? xf[q].spec : nullptr; }
   template <int SIGN>
   AF_HD void put(const cx* spec, int q, int m, cx v) const {
-    const cx p = spec ? conjc(cmul_s<SIGN>(v, ldcx(spec + m))) : make_cx(0.f, 0.f);
+    const cx p = spec ? conjc(cmul_s<SIGN>(v, spec_at(spec, M, m))) : make_cx(0.f, 0.f);
     nxt[ipos(m >> glogG, q * G + (m & (G - 1)), GL)] = p;
   }
 };
@@ -364,7 +422,7 @@ struct BlueOut {
   const FXform* xf;
   AF_HD const FXform* at(int q) const { return xf + q; }
   AF_HD void operator()(const FXform* x, int, int m, cx v, float& loss) const {
-    if (m < x->n) sk.put(x->off + m, cmul_s<SIGN>(conjc(v), chirp_at(*x, m)), loss);
+    if (m < x->n) sk.put(x->off + m, cmul_s<SIGN>(conjc(v), chirp_at<true>(*x, x->ct, m)), loss);
   }
 };
 
@@ -373,18 +431,16 @@ struct BlueOut {
 // FFT), y = a (.) conj(.) for the first n bins.  Q transforms sharing M.
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
   const int M = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
-  const FXform* xf = A.xf + it.first;
   const int cnt = it.count;
   ex.phase_async([&](int tid) {
     for (int i = tid; i < Q * M; i += T) {
       const int q = (int)fdiv((unsigned)i, S.ndiv);
       const int e = i - q * M;
       cx v = make_cx(0.f, 0.f);
-      if (q < cnt && e < xf[q].n) v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at(xf[q], e));
+      if (q < cnt && e < xf[q].n) v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at<true>(xf[q], xf[q].ct, e));
       m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
     }
     copy_tables(tid, T, S, m);
@@ -395,6 +451,7 @@ AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
   BlueMidS<SIGN> mid;
   mid.xf = xf;
   mid.cnt = cnt;
+  mid.M = M;
   mid.nxt = nxt;
   mid.glogG = glogG;
   mid.G = G;
@@ -407,28 +464,36 @@ AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
 
 // Multi-pass items work on one transform: columns [c0, c0 + cn) or lines
 // [c0, c0 + cn) of its n1 x n2 matrix (element (j1, j2) at j1 n2 + j2); the
-// shape's line FFT has GL lines (a power of two, cn <= GL).
-//
+// shape's line FFT has GL lines (a power of two, cn <= GL).  The item stages
+// the transform's three-level tables of W_N (wt) and W_2n (ct) with its loads.
+AF_HD void copy_multi_tables(int tid, int T, const FShape& S, const FSmem& m, const FXform& x) {
+  copy_tables(tid, T, S, m);
+  if (x.wt) copy_table(tid, T, m.wt3, x.wt, AFF_TL3);
+  if (x.ct) copy_table(tid, T, m.ct3, x.ct, AFF_TL3);
+}
+
 // FK_COLS (four-step pass A, Planned.hs:525-557) and FK_BCOLS (Bluestein
 // pass A): column FFT_n1 of x (FK_BCOLS: of a (.) x zero padded), twiddle
 // W_N^(j2 k1), stored column-contiguous: ws[j2 n1 + k1].
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, cx* sm, bool blue) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm, bool blue) {
   const FSmem m = smem_of(S, sm);
-  const FXform& x = A.xf[it.first];
+  const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
   const int n2 = x.n2, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    for (int i = tid; i < L * GL; i += T) {
-      const int e = i >> glogC, c = i & (GL - 1);
-      const int j = e * n2 + c0 + c;  // natural index of element e of column c0 + c
-      if (c >= cn) m.a[i] = make_cx(0.f, 0.f);
-      else if (!blue) cp_async8(m.a + i, A.in + x.off + j);
-      else m.a[i] = j < x.n ? cmul_s<SIGN>(ldcx(A.in + x.off + j), chirp_at(x, j)) : make_cx(0.f, 0.f);
+    if (!blue) {
+      load_lines<false>(tid, T, m.a, GL, glogC, A.in + x.off + c0, n2, L, cn);
+    } else {
+      for (int i = tid; i < L * GL; i += T) {
+        const int e = i >> glogC, c = i & (GL - 1);
+        const int j = e * n2 + c0 + c;  // natural index of element e of column c0 + c
+        m.a[i] = c < cn && j < x.n ? cmul_s<SIGN>(ldcx(A.in + x.off + j), chirp_at<true>(x, x.ct, j))
+                                   : make_cx(0.f, 0.f);
+      }
     }
-    copy_tables(tid, T, S, m);
+    copy_multi_tables(tid, T, S, m, x);
   });
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   ex.phase([&](int tid) {
@@ -436,7 +501,7 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, cx* sm, bool blue) 
       const int c = (int)fdiv((unsigned)u, S.L1div);
       const int k1 = u - c * L;
       const int j2 = c0 + c;
-      const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tw2(x.wt, (unsigned)(j2 * k1)));
+      const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
       A.ws[x.ws + (i64)j2 * L + k1] = v;
     }
   });
@@ -446,17 +511,13 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, cx* sm, bool blue) 
 // ws[j2 n1 + k1]; FFT_n2; X[k1 + n1 k2] to the output.
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
-  const FXform& x = A.xf[it.first];
+  const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int n1 = x.n1, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    for (int i = tid; i < L * GL; i += T) {
-      const int e = i >> glogR, l = i & (GL - 1);
-      m.a[i] = l < cn ? ldws(A.ws + x.ws + (i64)e * n1 + c0 + l) : make_cx(0.f, 0.f);
-    }
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn);
     copy_tables(tid, T, S, m);
   });
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
@@ -476,26 +537,23 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
 // this pass still read the first).
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
-  const FXform& x = A.xf[it.first];
+  const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int M1 = x.n1, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    for (int i = tid; i < L * GL; i += T) {
-      const int e = i >> glogR, l = i & (GL - 1);
-      m.a[i] = l < cn ? ldws(A.ws + x.ws + (i64)e * M1 + c0 + l) : make_cx(0.f, 0.f);
-    }
-    copy_tables(tid, T, S, m);
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn);
+    copy_multi_tables(tid, T, S, m, x);
   });
   cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   ex.phase([&](int tid) {
+#pragma unroll 4
     for (int u = tid; u < L * GL; u += T) {
       const int k2 = u >> glogR, l = u & (GL - 1);
       cx p = make_cx(0.f, 0.f);
-      if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], ldcx(x.spec + c0 + l + (i64)M1 * k2)));
+      if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + M1 * k2)));
       nxt[ipos(k2, l, GL)] = p;
     }
   });
@@ -505,7 +563,8 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
       const int l = (int)fdiv((unsigned)u, S.L1div);
       const int j2 = u - l * L;
       const int k1 = c0 + l;
-      A.ws[x.ws + x.M + (i64)k1 * L + j2] = cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tw2(x.wt, (unsigned)(j2 * k1)));
+      A.ws[x.ws + x.M + (i64)k1 * L + j2] =
+          cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
     }
   });
 }
@@ -514,18 +573,14 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
 // ws[M + k1 M2 + j2]; FFT_M1; y_m = a_m (.) conj(.) at m = j1 M2 + j2 < n.
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
-  const FShape& S = A.shapes[it.shape];
+AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
-  const FXform& x = A.xf[it.first];
+  const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
   const int M2 = x.n2, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    for (int i = tid; i < L * GL; i += T) {
-      const int e = i >> glogC, c = i & (GL - 1);
-      m.a[i] = c < cn ? ldws(A.ws + x.ws + x.M + (i64)e * M2 + c0 + c) : make_cx(0.f, 0.f);
-    }
-    copy_tables(tid, T, S, m);
+    load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn);
+    copy_multi_tables(tid, T, S, m, x);
   });
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
@@ -533,22 +588,23 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
     for (int u = tid; u < L * GL; u += T) {
       const int j1 = u >> glogC, c = u & (GL - 1);
       const int j = j1 * M2 + c0 + c;
-      if (c < cn && j < x.n) sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at(x, j)), loss);
+      if (c < cn && j < x.n)
+        sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
     }
   });
 }
 
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void run_item(E& ex, const FArgs& A, const FItem& it, cx* sm) {
+AF_HD void run_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   switch (it.kind) {
-    case FK_BLUE: blue_item<T, SIGN>(ex, A, it, sm); break;
-    case FK_COLS: cols_item<T, SIGN>(ex, A, it, sm, false); break;
-    case FK_BCOLS: cols_item<T, SIGN>(ex, A, it, sm, true); break;
-    case FK_ROWS: rows_item<T, SIGN>(ex, A, it, sm); break;
-    case FK_BROWS: brows_item<T, SIGN>(ex, A, it, sm); break;
-    case FK_BCOLS2: bcols2_item<T, SIGN>(ex, A, it, sm); break;
-    default: direct_item<T, SIGN>(ex, A, it, sm); break;
+    case FK_BLUE: blue_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_COLS: cols_item<T, SIGN>(ex, A, it, S, xf, sm, false); break;
+    case FK_BCOLS: cols_item<T, SIGN>(ex, A, it, S, xf, sm, true); break;
+    case FK_ROWS: rows_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_BROWS: brows_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_BCOLS2: bcols2_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    default: direct_item<T, SIGN>(ex, A, it, S, xf, sm); break;
   }
 }
 
@@ -561,25 +617,41 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+// n 4-byte words from global to shared memory
+__device__ __forceinline__ void copy_words(void* dst, const void* src, int n) {
+  const unsigned* s = reinterpret_cast<const unsigned*>(src);
+  unsigned* d = reinterpret_cast<unsigned*>(dst);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = __ldg(s + i);
+}
 #endif
 
 // Persistent executor: every CTA takes the next item of the queue (items
-// wait only for items earlier in the queue, which CTAs already hold, so the
-// launch always completes).  A wait polls its counter at most spin_limit
-// times; then the CTA records FE_TIMEOUT and leaves, and the items that
-// depend on it time out in turn.
+// wait only for items earlier in the queue, and the smallest unfinished item
+// is always held by a CTA that has started it or is about to, so the launch
+// always completes).  Thread 0 claims the CTA's following item while the
+// current one runs.  A wait polls its counter at most spin_limit times; then
+// the CTA records FE_TIMEOUT and leaves, and the items that depend on it
+// time out in turn.  The item's shape and transforms are staged in shared
+// memory (the shape only when it changes).
 template <int T, int SIGN>
 __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitems, unsigned* ctrs,
                                                               long long spin_limit) {
   extern __shared__ float4 fsm4[];
+  __shared__ FShape s_shape;
+  __shared__ FXform s_xf[AFF_MAXQ];
+  __shared__ FItem s_it;
   __shared__ int s_item, s_ok;
   DevExec ex;
+  int loaded = -1;  // shape staged in s_shape (uniform across the CTA)
+  int next = 0;     // thread 0: the item claimed for the next round
+  if (threadIdx.x == 0) next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
   for (;;) {
     if (threadIdx.x == 0) {
-      const int i = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+      const int i = next;
       int ok = 1;
       if (i < nitems) {
         const FItem it = A.items[i];
+        s_it = it;
         if (it.wait_ctr >= 0) {
           long long k = 0;
           while (ld_acquire(ctrs + it.wait_ctr) < (unsigned)it.wait_cnt) {
@@ -591,6 +663,7 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
             __nanosleep(64);
           }
         }
+        if (ok) next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
       }
       s_item = i;
       s_ok = ok;
@@ -598,19 +671,27 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
     __syncthreads();
     const int i = s_item;
     if (i >= nitems || !s_ok) break;
-    const FItem it = A.items[i];
-    run_item<T, SIGN>(ex, A, it, reinterpret_cast<cx*>(fsm4));
-    // publish this item's global stores before counting it done
-    __threadfence();
+    const FItem it = s_it;
+    if (it.shape != loaded) copy_words(&s_shape, A.shapes + it.shape, (int)(sizeof(FShape) / 4));
+    copy_words(s_xf, A.xf + it.first, it.count * (int)(sizeof(FXform) / 4));
     __syncthreads();
-    if (threadIdx.x == 0 && it.done_ctr >= 0) atomicAdd(ctrs + it.done_ctr, 1u);
+    loaded = it.shape;
+    run_item<T, SIGN>(ex, A, it, s_shape, s_xf, reinterpret_cast<cx*>(fsm4));
+    if (it.done_ctr >= 0) {
+      // every thread's stores of this item precede the barrier; thread 0's
+      // fence then publishes them before the count
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctrs + it.done_ctr, 1u);
+      }
+    }
   }
   if (A.w && A.loss) {
     __syncthreads();
     ex.finish_sum(A.loss, reinterpret_cast<double*>(fsm4), T);
   }
 }
-
 template <int T, int SIGN>
 static cudaError_t launch_fast_t(const FArgs& A, int nitems, size_t smem, unsigned* ctrs, int grid,
                                  long long spin_limit, cudaStream_t st) {
@@ -682,7 +763,8 @@ static int emulate_t(const FArgs& A, const FItem* items, int nitems, size_t smem
     const size_t bytes = (size_t)A.shapes[it.shape].smem;
     if (bytes > smem) throw FastError("item needs more shared memory than its launch");
     std::vector<cx> sm((bytes + sizeof(cx) - 1) / sizeof(cx));
-    run_item<T, SIGN>(ex, A, it, sm.data());
+    if (it.count < 1 || it.count > AFF_MAXQ) throw FastError("item transform count out of range");
+    run_item<T, SIGN>(ex, A, it, A.shapes[it.shape], A.xf + it.first, sm.data());
     if (it.done_ctr >= 0) ctr.at(it.done_ctr)++;
   }
   if (A.w && A.loss) ex.finish_sum(A.loss, nullptr, T);

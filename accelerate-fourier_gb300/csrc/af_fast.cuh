@@ -30,7 +30,7 @@ namespace af {
 
 // One Stockham pass of a line FFT: butterfly b reads elements b + m*nb and
 // writes q*p*R + k + m*p (k = b mod p, q = b div p) after the twiddles
-// W_{pR}^(k m), read from tw + k*R + m.
+// W_{pR}^(k m), read from tw + (m-1)*p + k.
 struct FPass {
   int R, p, nb, tw;
   int plog;  // log2 p when p is a power of two, else -1
@@ -87,20 +87,13 @@ template <> struct FVec<2> {
   }
 };
 
-// Pass twiddles of butterfly k: w[m] = W_{pR}^(k m), m = 1..R-1
+// Pass twiddles of butterfly k: w[m] = W_{pR}^(k m), m = 1..R-1, stored
+// m-major (entry (m-1) p + k) so that the lanes of a warp, which hold
+// consecutive k, read consecutive entries
 template <int R>
-AF_HD void pass_twiddles(const cx* t, cx* w) {
-  if constexpr (R % 2 == 0) {
+AF_HD void pass_twiddles(const cx* t, int k, int p, cx* w) {
 #pragma unroll
-    for (int m = 0; m < R; m += 2) {
-      const float4 v = *reinterpret_cast<const float4*>(t + m);
-      if (m > 0) w[m] = make_cx(v.x, v.y);
-      w[m + 1] = make_cx(v.z, v.w);
-    }
-  } else {
-#pragma unroll
-    for (int m = 1; m < R; ++m) w[m] = t[m];
-  }
+  for (int m = 1; m < R; ++m) w[m] = t[(m - 1) * p + k];
 }
 
 // One unit of a Stockham pass: butterfly b of the V lines starting at `line`.
@@ -122,7 +115,7 @@ AF_HD void fpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, const FP
   const int k = b - q * ps.p;
   if (k > 0) {
     cx w[R];
-    pass_twiddles<R>(tw + ps.tw + k * R, w);
+    pass_twiddles<R>(tw + ps.tw, k, ps.p, w);
 #pragma unroll
     for (int m = 1; m < R; ++m)
 #pragma unroll

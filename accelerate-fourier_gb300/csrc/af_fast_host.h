@@ -28,10 +28,15 @@ enum FKind {
 // pass.  Full-FFT shapes (FK_DIRECT, FK_BLUE) have n = L*G with GL = Q*G
 // (Q transforms per CTA) and the final radix-G pass; multi-pass shapes have
 // G = Q = 1 and GL lines (columns or rows) of one transform.
+// Multi-pass shapes (aux = 1) also stage two three-level root tables of
+// AFF_TL3 entries each.
+#define AFF_TL3 192
+// most transforms an item holds
+#define AFF_MAXQ 16
 struct FShape {
   FLine line;
   int kind;
-  int n, G, Q, GL, glog, V, LS, cap, ftwn;
+  int n, G, Q, GL, glog, V, LS, cap, ftwn, aux;
   int smem;  // shared-memory bytes an item of this shape uses
   FastDiv ndiv, L1div;
   const cx* tw;   // pass twiddles (line.twn entries)
@@ -58,9 +63,9 @@ struct FXform {
   int n;           // transform length
   int n1, n2;      // four-step split: n = n1 n2 (direct) or M = n1 n2 (Bluestein)
   int M;           // Bluestein convolution length
-  const cx* ct;    // Bluestein: two-level table of W_{2n} (chirp a_m = W_{2n}^(m^2))
-  const cx* wt;    // multi-pass: two-level table of W_n (direct) or W_M (Bluestein)
-  const cx* spec;  // Bluestein: spectrum FFT(b)/M of the conjugate chirp, M entries
+  const cx* ct;    // Bluestein: three-level table of W_{2n} (chirp a_m = W_{2n}^(m^2))
+  const cx* wt;    // multi-pass: three-level table of W_n (direct) or W_M (Bluestein)
+  const cx* spec;  // Bluestein: spectrum FFT(b)/M of the conjugate chirp, entries 0..M/2
   ModN mod2n;      // reduction mod 2n
 };
 
@@ -80,7 +85,7 @@ enum { RS_STOCK = 0, RS_LINEAR = 1 };
 struct RootSeg {
   i64 off, count;  // destination offset and entry count
   int kind;
-  i64 a, b;  // RS_STOCK: p, R;  RS_LINEAR: entry i = W_a^(i b)
+  i64 a, b;  // RS_STOCK: p, R (entry (m-1) p + k = W_{pR}^(k m));  RS_LINEAR: entry i = W_a^(i b)
 };
 
 struct FastError : std::runtime_error {

@@ -59,12 +59,12 @@ static void make_line(FLine& ln, int L, std::vector<RootSeg>* segs, i64 base) {
     if (p > 1) {
       RootSeg s;
       s.off = base + tw;
-      s.count = (i64)p * ps.R;
+      s.count = (i64)p * (ps.R - 1);
       s.kind = RS_STOCK;
       s.a = p;
       s.b = ps.R;
       segs->push_back(s);
-      tw += (int)even_up((i64)p * ps.R);
+      tw += (int)even_up((i64)p * (ps.R - 1));
     }
     p *= rs[j];
   }
@@ -90,7 +90,7 @@ struct FastBatch {
   std::vector<RootSeg> segs;
   std::vector<SpecJob> specs;
   i64 tab_elems = 0;
-  std::map<i64, i64> two_level;      // N -> offset of the two-level table of W_N
+  std::map<i64, i64> tl3_of;         // N -> offset of the three-level table of W_N
   std::map<i64, i64> spec_of;        // n -> offset of its Bluestein spectrum
   std::map<std::pair<int, int>, int> line_shapes;  // (L, GL) -> shape
   std::vector<FItem> queue;  // the persistent launch's items, in order
@@ -124,28 +124,28 @@ struct FastBatch {
 };
 
 // Every CTA of the persistent launch has 256 threads and the same shared
-// memory: three fit one SM (228 KB, less 1 KB reserved per CTA).
+// memory: three fit one SM (228 KB, less 1 KB reserved and the kernel's
+// 1.7 KB of staged descriptors per CTA).
 static const int kThreads = 256;
-static const int kCtaSmem = 76288;
+static const int kCtaSmem = 74752;
 static const int kDirectTarget = 4096;  // elements per CTA the items aim at
 static const int kMaxSmem = kCtaSmem;
 
 static size_t shape_smem(const FShape& s) {
-  return sizeof(cx) * (size_t)(2 * s.cap + s.line.twn + s.ftwn + 16);
+  return sizeof(cx) * (size_t)(2 * s.cap + s.line.twn + s.ftwn + (s.aux ? 2 * AFF_TL3 : 0) + 16);
 }
 
-
-static i64 table_two_level(FastBatch* B, i64 N) {
-  auto it = B->two_level.find(N);
-  if (it != B->two_level.end()) return it->second;
+// The three-level root table of W_N (t < 2^18): W_N^j, W_N^(64 j), W_N^(4096 j), j < 64.
+static i64 table_tl3(FastBatch* B, i64 N) {
+  if (N > ((i64)1 << 18)) throw FastError("three-level root tables cover lengths up to 2^18");
+  auto it = B->tl3_of.find(N);
+  if (it != B->tl3_of.end()) return it->second;
   const i64 off = B->tab_elems;
-  const i64 H = (N + 255) / 256;
-  RootSeg lo{off, 256, RS_LINEAR, N, 1};
-  RootSeg hi{off + 256, H, RS_LINEAR, N, 256};
-  B->segs.push_back(lo);
-  B->segs.push_back(hi);
-  B->tab_elems += even_up(256 + H);
-  B->two_level[N] = off;
+  B->segs.push_back(RootSeg{off, 64, RS_LINEAR, N, 1});
+  B->segs.push_back(RootSeg{off + 64, 64, RS_LINEAR, N, 64});
+  B->segs.push_back(RootSeg{off + 128, 64, RS_LINEAR, N, 4096});
+  B->tab_elems += AFF_TL3;
+  B->tl3_of[N] = off;
   return off;
 }
 
@@ -156,6 +156,7 @@ static void finish_shape(FShape& s) {
   s.glog = gl;
   s.LS = line_stride(s.line.L);
   s.cap = (int)even_up(std::max<i64>((i64)s.GL * s.line.L, (i64)s.GL * s.LS));
+  s.aux = s.kind < 0 ? 1 : 0;
   s.ndiv = make_fastdiv((unsigned)s.n);
   s.L1div = make_fastdiv((unsigned)s.line.L);
   s.smem = (int)shape_smem(s);
@@ -231,7 +232,7 @@ static i64 full_smem(i64 n, int Q) {
   const i64 L1 = n / G;
   i64 twn = 0, p = 1;
   for (int r : line_radices((int)L1)) {
-    if (p > 1) twn += even_up(p * r);
+    if (p > 1) twn += even_up(p * (r - 1));
     p *= r;
   }
   const i64 cap = even_up(std::max<i64>((i64)Q * n, (i64)Q * G * line_stride((int)L1)));
@@ -262,7 +263,7 @@ static i64 spectrum(FastBatch* B, i64 n, i64 M) {
   if (it != B->spec_of.end()) return it->second;
   const i64 off = B->tab_elems;
   B->specs.push_back(SpecJob{n, M, off});
-  B->tab_elems += even_up(M);
+  B->tab_elems += even_up(M / 2 + 1);  // the spectrum is even: entries 0..M/2
   B->spec_of[n] = off;
   return off;
 }
@@ -374,7 +375,7 @@ static void plan_batch(FastBatch* B) {
         if (kind == FK_BLUE) {
           x.M = (int)len;
           x.mod2n = make_modn((unsigned long long)(2 * n));
-          ct = table_two_level(B, 2 * n);
+          ct = table_tl3(B, 2 * n);
           spec = spectrum(B, n, len);
         }
         push_xf(B, x, ct, -1, spec);
@@ -395,13 +396,14 @@ static void plan_batch(FastBatch* B) {
     x.n2 = (int)n2;
     x.M = (int)N;
     x.ws = B->ws_elems;
-    const i64 wsn = even_up(N) * (blue ? 2 : 1);  // Bluestein: pass R writes a second region
+    // Bluestein: pass R writes a second region; regions start on 128-byte lines
+    const i64 wsn = ((N + 15) & ~(i64)15) * (blue ? 2 : 1);
     B->ws_elems += wsn;
     i64 ct = -1, spec = -1;
-    const i64 wt = table_two_level(B, N);
+    const i64 wt = table_tl3(B, N);
     if (blue) {
       x.mod2n = make_modn((unsigned long long)(2 * n));
-      ct = table_two_level(B, 2 * n);
+      ct = table_tl3(B, 2 * n);
       spec = spectrum(B, n, N);
     }
     const int xi = (int)B->xf.size();
@@ -468,9 +470,10 @@ __global__ void chirp_vec_kernel(double2* v, i64 n, i64 M, i64 count) {
   }
 }
 
+// entries 0..M/2 of the spectrum (the rest mirror them), scaled by 1/M and rounded
 __global__ void spec_round_kernel(const double2* V, cx* out, i64 M) {
   const double s = 1.0 / (double)M;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < M; i += (i64)gridDim.x * blockDim.x)
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i <= M / 2; i += (i64)gridDim.x * blockDim.x)
     out[i] = make_cx((float)(V[i].x * s), (float)(V[i].y * s));
 }
 
@@ -507,7 +510,7 @@ static void gen_spectra(FastBatch* B, cudaStream_t st) {
         if (m) v[j.M - m] = v[m];
       }
       host_fft64(v, -1);
-      for (i64 k = 0; k < j.M; ++k)
+      for (i64 k = 0; k <= j.M / 2; ++k)
         B->htab[j.off + k] = make_cx((float)(v[k].x / (double)j.M), (float)(v[k].y / (double)j.M));
     }
     return;
