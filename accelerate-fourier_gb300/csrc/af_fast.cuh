@@ -31,9 +31,12 @@ namespace af {
 // One Stockham pass of a line FFT: butterfly b reads elements b + m*nb and
 // writes q*p*R + k + m*p (k = b mod p, q = b div p) after the twiddles
 // W_{pR}^(k m), read from tw + (m-1)*p + k.
+// V: lines per unit of the pass (1 or 2, chosen so that the units spread
+// evenly over the CTA's threads); glog = log2(GL / V).
 struct FPass {
   int R, p, nb, tw;
   int plog;  // log2 p when p is a power of two, else -1
+  int V, glog;
   FastDiv pdiv;
 };
 struct FLine {

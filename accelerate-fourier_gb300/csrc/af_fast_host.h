@@ -23,7 +23,7 @@ enum FKind {
 };
 
 // A shape: what every transform of an item shares.  The line FFT has length
-// L over GL interleaved lines (V lines per unit, glog = log2(GL / V));
+// L over GL interleaved lines;
 // buffers hold `cap` elements each; LS is the line-major stride of the last
 // pass.  Full-FFT shapes (FK_DIRECT, FK_BLUE) have n = L*G with GL = Q*G
 // (Q transforms per CTA) and the final radix-G pass; multi-pass shapes have
@@ -36,7 +36,7 @@ enum FKind {
 struct FShape {
   FLine line;
   int kind;
-  int n, G, Q, GL, glog, V, LS, cap, ftwn, aux;
+  int n, G, Q, GL, LS, cap, ftwn, aux;
   int smem;  // shared-memory bytes an item of this shape uses
   FastDiv ndiv, L1div;
   const cx* tw;   // pass twiddles (line.twn entries)

@@ -149,11 +149,28 @@ static i64 table_tl3(FastBatch* B, i64 N) {
   return off;
 }
 
+static int ilog2_up(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
+// Lines per unit of each pass: two lines share the twiddle loads and move as
+// 16-byte vectors, but one line per unit wins when it spreads the units
+// over the threads in fewer rounds.
+static void choose_vectors(FShape& s) {
+  for (int j = 0; j < s.line.npass; ++j) {
+    FPass& ps = s.line.pass[j];
+    const i64 u1 = (i64)ps.nb * s.GL;
+    const i64 r1 = (u1 + kThreads - 1) / kThreads;
+    const i64 r2 = (u1 / 2 + kThreads - 1) / kThreads;
+    ps.V = (s.GL >= 2 && 2 * r2 * 17 <= r1 * 20) ? 2 : 1;  // a two-line unit costs about 1.7 one-line units
+    ps.glog = ilog2_up(s.GL / ps.V);
+  }
+}
+
 static void finish_shape(FShape& s) {
-  s.V = s.GL >= 2 ? 2 : 1;
-  int gl = 0;
-  while ((1 << gl) < s.GL / s.V) ++gl;
-  s.glog = gl;
+  choose_vectors(s);
   s.LS = line_stride(s.line.L);
   s.cap = (int)even_up(std::max<i64>((i64)s.GL * s.line.L, (i64)s.GL * s.LS));
   s.aux = s.kind < 0 ? 1 : 0;
