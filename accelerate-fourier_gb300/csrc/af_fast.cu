@@ -433,148 +433,171 @@ struct BlueOut {
 //     read the first).
 //   FK_BCOLS2 (Bluestein pass A'): columns j2, element k1 at ws[M + k1 M2 +
 //     j2]; FFT_M1; y_m = a_m (.) conj(.) at m = j1 M2 + j2 < n.
-// The line FFT has a single call site, so its passes are compiled once for
-// every kind.
+// Each phase reads the item's parameters from its descriptors (in shared
+// memory on the device) rather than keeping them live across the line FFT,
+// which has a single call site so that its passes are compiled once.
+
+// load phase of every kind (with the table copies)
+template <int T, int SIGN>
+AF_HD void item_load(int tid, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = xf[0];
+  const int GL = S.GL, glogL = ilog2i(GL);
+  const int kind = it.kind;
+  const i64 all = (i64)1 << 62;
+  switch (kind) {
+    case FK_DIRECT:
+      if (S.Q == 1) {  // one transform: its natural order is the layout
+        load_contiguous(tid, T, m.a, A.in + x.off, S.n);
+      } else {
+        const int G = S.G, glogG = ilog2i(G);
+        for (int i = tid; i < S.Q * S.n; i += T) {
+          const int q = (int)fdiv((unsigned)i, S.ndiv);
+          const int e = i - q * S.n;
+          const int pos = ipos(e >> glogG, q * G + (e & (G - 1)), GL);
+          if (q < it.count) cp_async8(m.a + pos, A.in + xf[q].off + e);
+          else m.a[pos] = make_cx(0.f, 0.f);
+        }
+      }
+      break;
+    case FK_BLUE: {
+      const int G = S.G, glogG = ilog2i(G);
+      for (int i = tid; i < S.Q * S.n; i += T) {
+        const int q = (int)fdiv((unsigned)i, S.ndiv);
+        const int e = i - q * S.n;
+        cx v = make_cx(0.f, 0.f);
+        if (q < it.count && e < xf[q].n)
+          v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at<true>(xf[q], xf[q].ct, e));
+        m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
+      }
+      break;
+    }
+    case FK_COLS:
+      load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + it.c0, x.n2, S.line.L, it.cn, all);
+      break;
+    case FK_BCOLS:
+      load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + it.c0, x.n2, S.line.L, it.cn, (i64)x.n - it.c0);
+      break;
+    case FK_ROWS:
+    case FK_BROWS:
+      load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + it.c0, x.n1, S.line.L, it.cn, all);
+      break;
+    default:  // FK_BCOLS2
+      load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + x.M + it.c0, x.n2, S.line.L, it.cn, all);
+      break;
+  }
+  if (kind >= FK_COLS) copy_multi_tables(tid, T, S, m, x);
+  else copy_tables(tid, T, S, m);
+}
+
+// FK_BCOLS: the chirp a_j on the loaded x_j
+template <int T, int SIGN>
+AF_HD void item_chirp_in(int tid, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = xf[0];
+  const int GL = S.GL, glogL = ilog2i(GL);
+  for (int i = tid; i < S.line.L * GL; i += T) {
+    const int e = i >> glogL, c = i & (GL - 1);
+    const int j = e * x.n2 + it.c0 + c;
+    if (c < it.cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
+  }
+}
+
+// between the two FFTs of FK_BLUE and FK_BROWS: the spectrum product,
+// conjugated, into the other buffer `oth`
+template <int T, int SIGN>
+AF_HD void item_mid(int tid, const FItem& it, const FShape& S, const FXform* xf, cx* sm, const cx* res, cx* oth,
+                    float& loss) {
+  const FSmem m = smem_of(S, sm);
+  const int GL = S.GL;
+  if (it.kind == FK_BLUE) {
+    const int LS = S.line.npass ? S.LS : 1;
+    BlueMid<SIGN> mid{xf, it.count, S.n, oth, ilog2i(S.G), S.G, GL};
+    final_any<SIGN>(tid, T, S.Q, S, res, LS, m.ftw, mid, loss);
+    return;
+  }
+  const FXform& x = xf[0];
+  const int glogL = ilog2i(GL), c0 = it.c0, cn = it.cn;
+#pragma unroll 4
+  for (int u = tid; u < S.line.L * GL; u += T) {
+    const int k2 = u >> glogL, l = u & (GL - 1);
+    cx p = make_cx(0.f, 0.f);
+    if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + x.n1 * k2)));
+    oth[ipos(k2, l, GL)] = p;
+  }
+}
+
+// store phase of every kind
+template <int T, int SIGN>
+AF_HD void item_end(int tid, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm,
+                    const cx* res, float& loss) {
+  const FSmem m = smem_of(S, sm);
+  const Sink sk{A.out, A.w};
+  const FXform& x = xf[0];
+  const int L = S.line.L, GL = S.GL, glogL = ilog2i(GL), c0 = it.c0, cn = it.cn;
+  switch (it.kind) {
+    case FK_DIRECT: {
+      DirectOut o{sk, xf};
+      final_any<SIGN>(tid, T, it.count, S, res, S.line.npass ? S.LS : 1, m.ftw, o, loss);
+      break;
+    }
+    case FK_BLUE: {
+      BlueOut<SIGN> o{sk, xf};
+      final_any<SIGN>(tid, T, it.count, S, res, S.line.npass ? S.LS : 1, m.ftw, o, loss);
+      break;
+    }
+    case FK_COLS:
+    case FK_BCOLS:
+      for (int u = tid; u < cn * L; u += T) {
+        const int c = (int)fdiv((unsigned)u, S.L1div);
+        const int k1 = u - c * L;
+        const int j2 = c0 + c;
+        A.ws[x.ws + (i64)j2 * L + k1] = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
+      }
+      break;
+    case FK_ROWS:
+      for (int u = tid; u < L * GL; u += T) {
+        const int k2 = u >> glogL, l = u & (GL - 1);
+        if (l < cn) sk.put(x.off + c0 + l + (i64)x.n1 * k2, res[lpos(k2, l, S.LS)], loss);
+      }
+      break;
+    case FK_BROWS:
+      for (int u = tid; u < cn * L; u += T) {
+        const int l = (int)fdiv((unsigned)u, S.L1div);
+        const int j2 = u - l * L;
+        const int k1 = c0 + l;
+        A.ws[x.ws + x.M + (i64)k1 * L + j2] =
+            cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
+      }
+      break;
+    default:  // FK_BCOLS2
+      for (int u = tid; u < L * GL; u += T) {
+        const int j1 = u >> glogL, c = u & (GL - 1);
+        const int j = j1 * x.n2 + c0 + c;
+        if (c < cn && j < x.n)
+          sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
+      }
+      break;
+  }
+}
+
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
 AF_HD void run_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
-  const FSmem m = smem_of(S, sm);
-  const int kind = it.kind;
-  const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogL = ilog2i(GL);
-  const int G = S.G, glogG = ilog2i(G), Q = S.Q, cnt = it.count;
-  const int c0 = it.c0, cn = it.cn;
-  const i64 all = (i64)1 << 62;
-  ex.phase_async([&](int tid) {
-    switch (kind) {
-      case FK_DIRECT:
-        if (Q == 1) {  // one transform: its natural order is the layout
-          load_contiguous(tid, T, m.a, A.in + x.off, S.n);
-        } else {
-          for (int i = tid; i < Q * S.n; i += T) {
-            const int q = (int)fdiv((unsigned)i, S.ndiv);
-            const int e = i - q * S.n;
-            const int pos = ipos(e >> glogG, q * G + (e & (G - 1)), GL);
-            if (q < cnt) cp_async8(m.a + pos, A.in + xf[q].off + e);
-            else m.a[pos] = make_cx(0.f, 0.f);
-          }
-        }
-        break;
-      case FK_BLUE:
-        for (int i = tid; i < Q * S.n; i += T) {
-          const int q = (int)fdiv((unsigned)i, S.ndiv);
-          const int e = i - q * S.n;
-          cx v = make_cx(0.f, 0.f);
-          if (q < cnt && e < xf[q].n)
-            v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at<true>(xf[q], xf[q].ct, e));
-          m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
-        }
-        break;
-      case FK_COLS:
-        load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + c0, x.n2, L, cn, all);
-        break;
-      case FK_BCOLS:
-        load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + c0, x.n2, L, cn, (i64)x.n - c0);
-        break;
-      case FK_ROWS:
-      case FK_BROWS:
-        load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + c0, x.n1, L, cn, all);
-        break;
-      default:  // FK_BCOLS2
-        load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + x.M + c0, x.n2, L, cn, all);
-        break;
-    }
-    if (kind >= FK_COLS) copy_multi_tables(tid, T, S, m, x);
-    else copy_tables(tid, T, S, m);
-  });
-  if (kind == FK_BCOLS) {  // the chirp a_j on the loaded x_j
-    ex.phase([&](int tid) {
-      for (int i = tid; i < L * GL; i += T) {
-        const int e = i >> glogL, c = i & (GL - 1);
-        const int j = e * x.n2 + c0 + c;
-        if (c < cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
-      }
-    });
-  }
-  const int nfft = (kind == FK_BLUE || kind == FK_BROWS) ? 2 : 1;
-  const int LS = S.line.npass ? S.LS : 1;  // no pass: the load layout read as line-major with LS 1
-  cx* src = m.a;
-  cx* dst = m.b;
+  ex.phase_async([&](int tid) { item_load<T, SIGN>(tid, A, it, S, xf, sm); });
+  if (it.kind == FK_BCOLS) ex.phase([&](int tid) { item_chirp_in<T, SIGN>(tid, it, S, xf, sm); });
+  const int nfft = (it.kind == FK_BLUE || it.kind == FK_BROWS) ? 2 : 1;
+  cx* src = sm;
+  cx* dst = sm + S.cap;
   for (int f = 0; f < nfft; ++f) {
-    cx* res = line_fft<T, SIGN>(ex, S, src, dst, m.tw);
-    cx* oth = res == m.a ? m.b : m.a;
-    if (f + 1 < nfft) {  // between the two FFTs: the spectrum product, into the other buffer
-      if (kind == FK_BLUE) {
-        BlueMid<SIGN> mid{xf, cnt, S.n, oth, glogG, G, GL};
-        ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, Q, S, res, LS, m.ftw, mid, loss); });
-      } else {
-        ex.phase([&](int tid) {
-#pragma unroll 4
-          for (int u = tid; u < L * GL; u += T) {
-            const int k2 = u >> glogL, l = u & (GL - 1);
-            cx p = make_cx(0.f, 0.f);
-            if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + x.n1 * k2)));
-            oth[ipos(k2, l, GL)] = p;
-          }
-        });
-      }
+    cx* res = line_fft<T, SIGN>(ex, S, src, dst, sm + 2 * S.cap);
+    cx* oth = res == sm ? sm + S.cap : sm;
+    if (f + 1 < nfft) {
+      ex.phase_sum([&](int tid, float& loss) { item_mid<T, SIGN>(tid, it, S, xf, sm, res, oth, loss); });
       src = oth;
       dst = res;
-      continue;
-    }
-    const Sink sk{A.out, A.w};
-    switch (kind) {
-      case FK_DIRECT: {
-        DirectOut o{sk, xf};
-        ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, o, loss); });
-        break;
-      }
-      case FK_BLUE: {
-        BlueOut<SIGN> o{sk, xf};
-        ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, o, loss); });
-        break;
-      }
-      case FK_COLS:
-      case FK_BCOLS:
-        ex.phase([&](int tid) {
-          for (int u = tid; u < cn * L; u += T) {
-            const int c = (int)fdiv((unsigned)u, S.L1div);
-            const int k1 = u - c * L;
-            const int j2 = c0 + c;
-            A.ws[x.ws + (i64)j2 * L + k1] =
-                cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-          }
-        });
-        break;
-      case FK_ROWS:
-        ex.phase_sum([&](int tid, float& loss) {
-          for (int u = tid; u < L * GL; u += T) {
-            const int k2 = u >> glogL, l = u & (GL - 1);
-            if (l < cn) sk.put(x.off + c0 + l + (i64)x.n1 * k2, res[lpos(k2, l, S.LS)], loss);
-          }
-        });
-        break;
-      case FK_BROWS:
-        ex.phase([&](int tid) {
-          for (int u = tid; u < cn * L; u += T) {
-            const int l = (int)fdiv((unsigned)u, S.L1div);
-            const int j2 = u - l * L;
-            const int k1 = c0 + l;
-            A.ws[x.ws + x.M + (i64)k1 * L + j2] =
-                cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-          }
-        });
-        break;
-      default:  // FK_BCOLS2
-        ex.phase_sum([&](int tid, float& loss) {
-          for (int u = tid; u < L * GL; u += T) {
-            const int j1 = u >> glogL, c = u & (GL - 1);
-            const int j = j1 * x.n2 + c0 + c;
-            if (c < cn && j < x.n)
-              sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
-          }
-        });
-        break;
+    } else {
+      ex.phase_sum([&](int tid, float& loss) { item_end<T, SIGN>(tid, A, it, S, xf, sm, res, loss); });
     }
   }
 }
