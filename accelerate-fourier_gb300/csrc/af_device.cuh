@@ -329,7 +329,7 @@ template <> struct Dft<8> {
 };
 
 // multiply by w16^m, m in 0..9
-__device__ __forceinline__ cx mul_w16(cx a, int m, rl sign) {
+AF_HD cx mul_w16(cx a, int m, rl sign) {
   switch (m) {
     case 0: return a;
     case 1: return cmul(a, make_cx(AF_C8, sign * AF_S8));
@@ -343,7 +343,7 @@ __device__ __forceinline__ cx mul_w16(cx a, int m, rl sign) {
 }
 
 template <> struct Dft<16> {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx*, int, int) {
+  static AF_HD void run(cx* u, rl sign, const cx*, int, int) {
     // 4 x 4: v_a = DFT4(u[a + 4m]); v_a[b] *= w16^(a b); y[b + 4c] = DFT4_a(v_a[b])
 #pragma unroll
     for (int a = 0; a < 4; ++a) dft4(u[a], u[a + 4], u[a + 8], u[a + 12], sign);

@@ -166,7 +166,10 @@ AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, in
     case 3: fpass_thread<3, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
     case 4: fpass_thread<4, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
     case 5: fpass_thread<5, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
-    default: fpass_thread<8, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    case 8: fpass_thread<8, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    default:  // 16: one line per unit (the planner never pairs lines at radix 16)
+      if (V == 1) fpass_thread<16, 1, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw);
+      break;
   }
 }
 

@@ -10,7 +10,7 @@
 #include <vector>
 
 #include "af_fast_host.h"
-#include "../../include/af.h"
+#include "af.h"
 #include "af_plan.h"
 
 namespace af {
@@ -25,11 +25,21 @@ static int trailing_zeros(i64 n) {
 }
 static i64 even_up(i64 v) { return (v + 1) & ~(i64)1; }
 
-// Radices of a 5-smooth line length: 8s first (the first pass has no
+// Planner choices the autotuner varies.
+struct FastTune {
+  int radix16 = 0;          // radix-16 passes where the length allows (else radix 8)
+  int gl_max = 16;          // most lines in one multi-pass item
+  int balance_v = 1;        // per-pass choice of lines per unit (else two whenever possible)
+  int target = 4096;        // elements one item aims at
+};
+
+// Radices of a 5-smooth line length: 16s or 8s first (the first pass has no
 // twiddles), then 5, 4, 3, 2.
-static std::vector<int> line_radices(int L) {
+static std::vector<int> line_radices(int L, bool r16) {
   std::vector<int> r;
   int m = L;
+  if (r16)
+    while (m % 16 == 0) { r.push_back(16); m /= 16; }
   while (m % 8 == 0) { r.push_back(8); m /= 8; }
   while (m % 5 == 0) { r.push_back(5); m /= 5; }
   if (m % 4 == 0) { r.push_back(4); m /= 4; }
@@ -41,10 +51,10 @@ static std::vector<int> line_radices(int L) {
 
 // Fills the line FFT of length L; returns the twiddle entries it needs and
 // appends their table segments (offsets relative to the shape's table).
-static void make_line(FLine& ln, int L, std::vector<RootSeg>* segs, i64 base) {
+static void make_line(FLine& ln, int L, std::vector<RootSeg>* segs, i64 base, bool r16) {
   memset(&ln, 0, sizeof ln);
   ln.L = L;
-  const std::vector<int> rs = line_radices(L);
+  const std::vector<int> rs = line_radices(L, r16);
   if ((int)rs.size() > AFF_MAXPASS) throw FastError("too many passes");
   int p = 1, tw = 0;
   ln.npass = (int)rs.size();
@@ -113,6 +123,7 @@ struct FastBatch {
   std::vector<FXform> hxf;
   std::vector<FItem> hitems;
   std::vector<cx> hws;
+  FastTune tune;
   ~FastBatch() {
     if (dtab) cudaFree(dtab);
     if (dws) cudaFree(dws);
@@ -128,7 +139,6 @@ struct FastBatch {
 // 1.7 KB of staged descriptors per CTA).
 static const int kThreads = 256;
 static const int kCtaSmem = 74752;
-static const int kDirectTarget = 4096;  // elements per CTA the items aim at
 static const int kMaxSmem = kCtaSmem;
 
 static size_t shape_smem(const FShape& s) {
@@ -158,19 +168,20 @@ static int ilog2_up(int v) {
 // Lines per unit of each pass: two lines share the twiddle loads and move as
 // 16-byte vectors, but one line per unit wins when it spreads the units
 // over the threads in fewer rounds.
-static void choose_vectors(FShape& s) {
+static void choose_vectors(FShape& s, bool balance) {
   for (int j = 0; j < s.line.npass; ++j) {
     FPass& ps = s.line.pass[j];
     const i64 u1 = (i64)ps.nb * s.GL;
     const i64 r1 = (u1 + kThreads - 1) / kThreads;
     const i64 r2 = (u1 / 2 + kThreads - 1) / kThreads;
-    ps.V = (s.GL >= 2 && 2 * r2 * 17 <= r1 * 20) ? 2 : 1;  // a two-line unit costs about 1.7 one-line units
+    // a two-line unit costs about 1.7 one-line units
+    ps.V = (s.GL >= 2 && ps.R != 16 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
     ps.glog = ilog2_up(s.GL / ps.V);
   }
 }
 
-static void finish_shape(FShape& s) {
-  choose_vectors(s);
+static void finish_shape(FShape& s, const FastTune& t) {
+  choose_vectors(s, t.balance_v != 0);
   s.LS = line_stride(s.line.L);
   s.cap = (int)even_up(std::max<i64>((i64)s.GL * s.line.L, (i64)s.GL * s.LS));
   s.aux = s.kind < 0 ? 1 : 0;
@@ -189,7 +200,7 @@ static int full_shape(FastBatch* B, int kind, i64 n, int Q) {
   s.G = 1 << std::min(trailing_zeros(n), 3);
   const int L1 = (int)(n / s.G);
   const i64 tw_base = B->tab_elems;
-  make_line(s.line, L1, &B->segs, tw_base);
+  make_line(s.line, L1, &B->segs, tw_base, B->tune.radix16 != 0);
   B->tab_elems += s.line.twn;
   // the final radix-G pass needs W_n^k1 (none when G = 1)
   s.ftwn = s.G > 1 ? (int)even_up(L1) : 0;
@@ -201,7 +212,7 @@ static int full_shape(FastBatch* B, int kind, i64 n, int Q) {
   B->tab_elems += s.ftwn;
   s.Q = Q;
   s.GL = Q * s.G;
-  finish_shape(s);
+  finish_shape(s, B->tune);
   B->shapes.push_back(s);
   B->shape_tw.push_back(tw_base);
   B->shape_ftw.push_back(ftw_base);
@@ -210,8 +221,11 @@ static int full_shape(FastBatch* B, int kind, i64 n, int Q) {
 
 // Line shape of the multi-pass schemes: FFT of length L over GL lines.
 static int line_shape(FastBatch* B, int L) {
-  int GL = 16;
-  while (GL > 2 && (i64)GL * L > kDirectTarget) GL /= 2;
+  // lines at most gl_max, GL * L at most the item target and within the
+  // shared memory of a CTA (two buffers of GL line-major rows)
+  int GL = B->tune.gl_max;
+  while (GL > 2 && ((i64)GL * L > B->tune.target || (i64)sizeof(cx) * 2 * GL * ((L | 1) + 1) > kMaxSmem * 7 / 8))
+    GL /= 2;
   auto key = std::make_pair(L, GL);
   auto it = B->line_shapes.find(key);
   if (it != B->line_shapes.end()) return it->second;
@@ -223,9 +237,9 @@ static int line_shape(FastBatch* B, int L) {
   s.Q = 1;
   s.GL = GL;
   const i64 tw_base = B->tab_elems;
-  make_line(s.line, L, &B->segs, tw_base);
+  make_line(s.line, L, &B->segs, tw_base, B->tune.radix16 != 0);
   B->tab_elems += s.line.twn;
-  finish_shape(s);
+  finish_shape(s, B->tune);
   B->shapes.push_back(s);
   B->shape_tw.push_back(tw_base);
   B->shape_ftw.push_back(tw_base);
@@ -244,11 +258,11 @@ static i64 four_step_n1(i64 n) {
 }
 
 // shared memory a full-FFT shape of length n with Q transforms per CTA needs
-static i64 full_smem(i64 n, int Q) {
+static i64 full_smem(i64 n, int Q, bool r16) {
   const int G = 1 << std::min(trailing_zeros(n), 3);
   const i64 L1 = n / G;
   i64 twn = 0, p = 1;
-  for (int r : line_radices((int)L1)) {
+  for (int r : line_radices((int)L1, r16)) {
     if (p > 1) twn += even_up(p * (r - 1));
     p *= r;
   }
@@ -353,18 +367,19 @@ static void order_queue(FastBatch* B, std::vector<MultiT>& multi, std::vector<FI
 }
 
 static void plan_batch(FastBatch* B) {
+  const bool r16 = B->tune.radix16 != 0;
   std::map<i64, std::vector<int>> direct_by_n, blue_by_M;
   std::vector<int> four, blue3;
   for (size_t i = 0; i < B->ns.size(); ++i) {
     const i64 n = B->ns[i];
     if (n == 0) continue;
     if (is_5smooth(n)) {
-      if (full_smem(n, 1) <= kMaxSmem) direct_by_n[n].push_back((int)i);
+      if (full_smem(n, 1, r16) <= kMaxSmem) direct_by_n[n].push_back((int)i);
       else if (four_step_n1(n)) four.push_back((int)i);
       else throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
     } else {
       const i64 M = blue_len(n);
-      if (full_smem(M, 1) <= kMaxSmem) blue_by_M[M].push_back((int)i);
+      if (full_smem(M, 1, r16) <= kMaxSmem) blue_by_M[M].push_back((int)i);
       else if (four_step_n1(M)) blue3.push_back((int)i);
       else throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
     }
@@ -372,8 +387,8 @@ static void plan_batch(FastBatch* B) {
   std::vector<FItem> singles;
   auto group_items = [&](int kind, i64 len, const std::vector<int>& idx) {
     int Q = 1;
-    while ((i64)Q * 2 * len <= kDirectTarget && Q * 2 <= (int)idx.size() && Q * 2 * 8 <= 128 &&
-           full_smem(len, Q * 2) <= kMaxSmem)
+    while ((i64)Q * 2 * len <= B->tune.target && Q * 2 <= (int)idx.size() && Q * 2 <= AFF_MAXQ &&
+           full_smem(len, Q * 2, r16) <= kMaxSmem)
       Q *= 2;
     const int si = full_shape(B, kind, len, Q);
     for (size_t j = 0; j < idx.size(); j += Q) {
@@ -614,10 +629,17 @@ static void bind_batch(FastBatch* B, cudaStream_t st) {
   fcheck(cudaStreamSynchronize(st), "batch upload");
 }
 
-FastBatch* fast_create(const i64* ns, i64 count, bool emu) {
+FastBatch* fast_create(const i64* ns, i64 count, bool emu, const int* tune, int ntune) {
   FastBatch* B = new FastBatch();
   try {
     B->emu = emu;
+    // tuning overrides in FastTune field order; a negative entry keeps the default
+    int* fields[] = {&B->tune.radix16, &B->tune.gl_max, &B->tune.balance_v, &B->tune.target};
+    for (int i = 0; i < ntune && i < 4; ++i)
+      if (tune[i] >= 0) *fields[i] = tune[i];
+    if (B->tune.gl_max < 2 || B->tune.gl_max > 128 || (B->tune.gl_max & (B->tune.gl_max - 1)))
+      throw FastError("lines per item must be a power of two in [2, 128]");
+    if (B->tune.target < 256 || B->tune.target > 8192) throw FastError("item target must be in [256, 8192]");
     B->ns.assign(ns, ns + count);
     B->offs.resize(count);
     i64 o = 0;
@@ -696,7 +718,19 @@ __attribute__((visibility("default"))) const char* afx_fast_error(void) { return
 __attribute__((visibility("default"))) int afx_fast_create(const int64_t* ns, int64_t count, int emulate,
                                                            void** out) {
   try {
-    *out = af::fast_create((const af::i64*)ns, count, emulate != 0);
+    *out = af::fast_create((const af::i64*)ns, count, emulate != 0, nullptr, 0);
+    return 0;
+  } catch (const std::exception& e) {
+    g_fast_err = e.what();
+    *out = nullptr;
+    return 1;
+  }
+}
+
+__attribute__((visibility("default"))) int afx_fast_create_tuned(const int64_t* ns, int64_t count, int emulate,
+                                                                 const int* tune, int ntune, void** out) {
+  try {
+    *out = af::fast_create((const af::i64*)ns, count, emulate != 0, tune, ntune);
     return 0;
   } catch (const std::exception& e) {
     g_fast_err = e.what();

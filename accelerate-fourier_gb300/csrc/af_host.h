@@ -7,7 +7,7 @@
 #include <tuple>
 #include <vector>
 
-#include "../../include/af.h"
+#include "af.h"
 #include "af_internal.h"
 #include "af_plan.h"
 
