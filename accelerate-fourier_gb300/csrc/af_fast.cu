@@ -319,13 +319,6 @@ AF_HD void copy_tables(int tid, int T, const FShape& S, const FSmem& m) {
   copy_table(tid, T, m.tw, S.tw, S.line.twn);
   copy_table(tid, T, m.ftw, S.ftw, S.ftwn);
 }
-// multi-pass items also stage the transform's three-level tables of W_N (wt)
-// and W_2n (ct)
-AF_HD void copy_multi_tables(int tid, int T, const FShape& S, const FSmem& m, const FXform& x) {
-  copy_tables(tid, T, S, m);
-  if (x.wt) copy_table(tid, T, m.wt3, x.wt, AFF_TL3);
-  if (x.ct) copy_table(tid, T, m.ct3, x.ct, AFF_TL3);
-}
 
 // n contiguous elements into shared memory: 16-byte copies when the source
 // is 16-byte aligned, else 8-byte copies
@@ -339,15 +332,12 @@ AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
 }
 
 // Lines [0, cn) of a strided matrix, rows e < L, into the interleaved layout
-// dst[e GL + c] = src[e stride + c]; lines cn..GL-1, and source positions
-// e stride + c >= lim, read as zero.  Pairs of lines move as 16-byte copies
-// at L2 when every pair is 16-byte aligned; otherwise one element at a time,
-// at L2 for workspace sources (WS: written by other CTAs of this launch, so
-// never read through L1).
+// dst[e GL + c] = src[e stride + c] (lines cn..GL-1 zero).  Pairs of lines move
+// as 16-byte copies at L2 when every pair is 16-byte aligned; otherwise one
+// element at a time, at L2 for workspace sources (WS: written by other CTAs
+// of this launch, so never read through L1).
 template <bool WS>
-AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn,
-                      i64 lim) {
-  const cx z = make_cx(0.f, 0.f);
+AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn) {
   const bool v16 = GL >= 2 && ((reinterpret_cast<unsigned long long>(src) & 15) == 0) && (stride % 2 == 0) &&
                    (cn % 2 == 0);
   if (v16) {
@@ -355,25 +345,19 @@ AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, 
     for (int i = tid; i < L * half; i += T) {
       const int e = i >> hlog, c = (i & (half - 1)) * 2;
       cx* d = dst + e * GL + c;
-      const i64 s = e * stride + c;
-      if (c < cn && s + 1 < lim) {
-        cp_async16(d, src + s);
-      } else if (c < cn && s < lim) {
-        if (WS) d[0] = ldws(src + s);
-        else cp_async8(d, src + s);
-        d[1] = z;
+      if (c < cn) {
+        cp_async16(d, src + e * stride + c);
       } else {
-        d[0] = z;
-        d[1] = z;
+        d[0] = make_cx(0.f, 0.f);
+        d[1] = make_cx(0.f, 0.f);
       }
     }
   } else {
     for (int i = tid; i < L * GL; i += T) {
       const int e = i >> glog, c = i & (GL - 1);
-      const i64 s = e * stride + c;
-      if (c >= cn || s >= lim) dst[i] = z;
-      else if (WS) dst[i] = ldws(src + s);
-      else cp_async8(dst + i, src + s);
+      if (c >= cn) dst[i] = make_cx(0.f, 0.f);
+      else if (WS) dst[i] = ldws(src + e * stride + c);
+      else cp_async8(dst + i, src + e * stride + c);
     }
   }
 }
@@ -386,20 +370,52 @@ struct DirectOut {
   AF_HD void operator()(i64 base, int, int m, cx v, float& loss) const { sk.put(base + m, v, loss); }
 };
 
+// FK_DIRECT: Q transforms of one 5-smooth length, loaded in natural order
+// (G interleaved lines each), line FFT, radix-G pass to the output.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
+  const int n = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
+  const int cnt = it.count;
+  ex.phase_async([&](int tid) {
+    if (Q == 1) {  // one transform: its natural order is the layout
+      load_contiguous(tid, T, m.a, A.in + xf[0].off, n);
+    } else {
+      for (int i = tid; i < Q * n; i += T) {
+        const int q = (int)fdiv((unsigned)i, S.ndiv);
+        const int e = i - q * n;
+        const int pos = ipos(e >> glogG, q * G + (e & (G - 1)), GL);
+        if (q < cnt) cp_async8(m.a + pos, A.in + xf[q].off + e);
+        else m.a[pos] = make_cx(0.f, 0.f);
+      }
+    }
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const int LS = S.line.npass ? S.LS : 1;  // no pass: the load layout read as line-major with LS 1
+  DirectOut f{Sink{A.out, A.w}, xf};
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, f, loss); });
+}
+
 // sinks of the Bluestein item: the spectrum product (conjugated) into the
 // other buffer, in the layout of the second FFT's input; and the chirp
 // product of the first n bins to the output
-template <int SIGN>
 struct BlueMid {
   const FXform* xf;
   int cnt, M;
   cx* nxt;
   int glogG, G, GL;
   AF_HD const cx* at(int q) const { return q < cnt ? xf[q].spec : nullptr; }
-  AF_HD void operator()(const cx* spec, int q, int m, cx v, float&) const {
+  template <int SIGN>
+  AF_HD void put(const cx* spec, int q, int m, cx v) const {
     const cx p = spec ? conjc(cmul_s<SIGN>(v, spec_at(spec, M, m))) : make_cx(0.f, 0.f);
     nxt[ipos(m >> glogG, q * G + (m & (G - 1)), GL)] = p;
   }
+};
+template <int SIGN>
+struct BlueMidS : BlueMid {
+  AF_HD void operator()(const cx* spec, int q, int m, cx v, float&) const { put<SIGN>(spec, q, m, v); }
 };
 template <int SIGN>
 struct BlueOut {
@@ -411,196 +427,188 @@ struct BlueOut {
   }
 };
 
-// One work item.  Kinds:
-//   FK_DIRECT: Q transforms of one 5-smooth length, loaded in natural order
-//     (G interleaved lines each), line FFT, radix-G pass to the output.
-//   FK_BLUE: Bluestein in one CTA (Planned.hs:760-773): u = a (.) x zero
-//     padded to M, FFT, times the spectrum, conjugate, FFT (= conj of the
-//     opposite-sign FFT), y = a (.) conj(.) for the first n bins; Q
-//     transforms sharing M.
-//   Multi-pass kinds work on one transform: columns [c0, c0 + cn) or lines
-//   [c0, c0 + cn) of its n1 x n2 matrix (element (j1, j2) at j1 n2 + j2);
-//   the shape's line FFT has GL lines (a power of two, cn <= GL).
-//   FK_COLS (four-step pass A, Planned.hs:525-557) and FK_BCOLS (Bluestein
-//     pass A): column FFT_n1 of x (FK_BCOLS: of a (.) x zero padded),
-//     twiddle W_N^(j2 k1), stored column-contiguous: ws[j2 n1 + k1].
-//   FK_ROWS (four-step pass B): lines k1 in [c0, c0 + cn), element j2 at
-//     ws[j2 n1 + k1]; FFT_n2; X[k1 + n1 k2] to the output.
-//   FK_BROWS (Bluestein pass R): lines k1, element j2 at ws[j2 M1 + k1];
-//     FFT_M2; times the spectrum at k1 + M1 k2 and conjugated; FFT_M2 again;
-//     twiddle W_M^(j2 k1); stored line-contiguous in the transform's second
-//     workspace region: ws[M + k1 M2 + j2] (other items of this pass still
-//     read the first).
-//   FK_BCOLS2 (Bluestein pass A'): columns j2, element k1 at ws[M + k1 M2 +
-//     j2]; FFT_M1; y_m = a_m (.) conj(.) at m = j1 M2 + j2 < n.
-// Each phase reads the item's parameters from its descriptors (in shared
-// memory on the device) rather than keeping them live across the line FFT,
-// which has a single call site so that its passes are compiled once.
-
-// load phase of every kind (with the table copies)
-template <int T, int SIGN>
-AF_HD void item_load(int tid, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+// FK_BLUE: Bluestein in one CTA (Planned.hs:760-773): u = a (.) x zero padded
+// to M, FFT, times the spectrum, conjugate, FFT (= conj of the opposite-sign
+// FFT), y = a (.) conj(.) for the first n bins.  Q transforms sharing M.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
-  const FXform& x = xf[0];
-  const int GL = S.GL, glogL = ilog2i(GL);
-  const int kind = it.kind;
-  const i64 all = (i64)1 << 62;
-  switch (kind) {
-    case FK_DIRECT:
-      if (S.Q == 1) {  // one transform: its natural order is the layout
-        load_contiguous(tid, T, m.a, A.in + x.off, S.n);
-      } else {
-        const int G = S.G, glogG = ilog2i(G);
-        for (int i = tid; i < S.Q * S.n; i += T) {
-          const int q = (int)fdiv((unsigned)i, S.ndiv);
-          const int e = i - q * S.n;
-          const int pos = ipos(e >> glogG, q * G + (e & (G - 1)), GL);
-          if (q < it.count) cp_async8(m.a + pos, A.in + xf[q].off + e);
-          else m.a[pos] = make_cx(0.f, 0.f);
-        }
-      }
-      break;
-    case FK_BLUE: {
-      const int G = S.G, glogG = ilog2i(G);
-      for (int i = tid; i < S.Q * S.n; i += T) {
-        const int q = (int)fdiv((unsigned)i, S.ndiv);
-        const int e = i - q * S.n;
-        cx v = make_cx(0.f, 0.f);
-        if (q < it.count && e < xf[q].n)
-          v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at<true>(xf[q], xf[q].ct, e));
-        m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
-      }
-      break;
+  const int M = S.n, G = S.G, GL = S.GL, Q = S.Q, glogG = ilog2i(G);
+  const int cnt = it.count;
+  ex.phase_async([&](int tid) {
+    for (int i = tid; i < Q * M; i += T) {
+      const int q = (int)fdiv((unsigned)i, S.ndiv);
+      const int e = i - q * M;
+      cx v = make_cx(0.f, 0.f);
+      if (q < cnt && e < xf[q].n) v = cmul_s<SIGN>(ldcx(A.in + xf[q].off + e), chirp_at<true>(xf[q], xf[q].ct, e));
+      m.a[ipos(e >> glogG, q * G + (e & (G - 1)), GL)] = v;
     }
-    case FK_COLS:
-      load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + it.c0, x.n2, S.line.L, it.cn, all);
-      break;
-    case FK_BCOLS:
-      load_lines<false>(tid, T, m.a, GL, glogL, A.in + x.off + it.c0, x.n2, S.line.L, it.cn, (i64)x.n - it.c0);
-      break;
-    case FK_ROWS:
-    case FK_BROWS:
-      load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + it.c0, x.n1, S.line.L, it.cn, all);
-      break;
-    default:  // FK_BCOLS2
-      load_lines<true>(tid, T, m.a, GL, glogL, A.ws + x.ws + x.M + it.c0, x.n2, S.line.L, it.cn, all);
-      break;
-  }
-  if (kind >= FK_COLS) copy_multi_tables(tid, T, S, m, x);
-  else copy_tables(tid, T, S, m);
+    copy_tables(tid, T, S, m);
+  });
+  const int LS = S.line.npass ? S.LS : 1;
+  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* nxt = res == m.a ? m.b : m.a;
+  BlueMidS<SIGN> mid;
+  mid.xf = xf;
+  mid.cnt = cnt;
+  mid.M = M;
+  mid.nxt = nxt;
+  mid.glogG = glogG;
+  mid.G = G;
+  mid.GL = GL;
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, Q, S, res, LS, m.ftw, mid, loss); });
+  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  BlueOut<SIGN> out{Sink{A.out, A.w}, xf};
+  ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, out, loss); });
 }
 
-// FK_BCOLS: the chirp a_j on the loaded x_j
-template <int T, int SIGN>
-AF_HD void item_chirp_in(int tid, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+// Multi-pass items work on one transform: columns [c0, c0 + cn) or lines
+// [c0, c0 + cn) of its n1 x n2 matrix (element (j1, j2) at j1 n2 + j2); the
+// shape's line FFT has GL lines (a power of two, cn <= GL).  The item stages
+// the transform's three-level tables of W_N (wt) and W_2n (ct) with its loads.
+AF_HD void copy_multi_tables(int tid, int T, const FShape& S, const FSmem& m, const FXform& x) {
+  copy_tables(tid, T, S, m);
+  if (x.wt) copy_table(tid, T, m.wt3, x.wt, AFF_TL3);
+  if (x.ct) copy_table(tid, T, m.ct3, x.ct, AFF_TL3);
+}
+
+// FK_COLS (four-step pass A, Planned.hs:525-557) and FK_BCOLS (Bluestein
+// pass A): column FFT_n1 of x (FK_BCOLS: of a (.) x zero padded), twiddle
+// W_N^(j2 k1), stored column-contiguous: ws[j2 n1 + k1].
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm, bool blue) {
   const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int GL = S.GL, glogL = ilog2i(GL);
-  for (int i = tid; i < S.line.L * GL; i += T) {
-    const int e = i >> glogL, c = i & (GL - 1);
-    const int j = e * x.n2 + it.c0 + c;
-    if (c < it.cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
-  }
+  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int n2 = x.n2, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    if (!blue) {
+      load_lines<false>(tid, T, m.a, GL, glogC, A.in + x.off + c0, n2, L, cn);
+    } else {
+      for (int i = tid; i < L * GL; i += T) {
+        const int e = i >> glogC, c = i & (GL - 1);
+        const int j = e * n2 + c0 + c;  // natural index of element e of column c0 + c
+        m.a[i] = c < cn && j < x.n ? cmul_s<SIGN>(ldcx(A.in + x.off + j), chirp_at<true>(x, x.ct, j))
+                                   : make_cx(0.f, 0.f);
+      }
+    }
+    copy_multi_tables(tid, T, S, m, x);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  ex.phase([&](int tid) {
+    for (int u = tid; u < cn * L; u += T) {
+      const int c = (int)fdiv((unsigned)u, S.L1div);
+      const int k1 = u - c * L;
+      const int j2 = c0 + c;
+      const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
+      A.ws[x.ws + (i64)j2 * L + k1] = v;
+    }
+  });
 }
 
-// between the two FFTs of FK_BLUE and FK_BROWS: the spectrum product,
-// conjugated, into the other buffer `oth`
-template <int T, int SIGN>
-AF_HD void item_mid(int tid, const FItem& it, const FShape& S, const FXform* xf, cx* sm, const cx* res, cx* oth,
-                    float& loss) {
+// FK_ROWS (four-step pass B): lines k1 in [c0, c0 + cn), element j2 at
+// ws[j2 n1 + k1]; FFT_n2; X[k1 + n1 k2] to the output.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
-  const int GL = S.GL;
-  if (it.kind == FK_BLUE) {
-    const int LS = S.line.npass ? S.LS : 1;
-    BlueMid<SIGN> mid{xf, it.count, S.n, oth, ilog2i(S.G), S.G, GL};
-    final_any<SIGN>(tid, T, S.Q, S, res, LS, m.ftw, mid, loss);
-    return;
-  }
   const FXform& x = xf[0];
-  const int glogL = ilog2i(GL), c0 = it.c0, cn = it.cn;
-#pragma unroll 4
-  for (int u = tid; u < S.line.L * GL; u += T) {
-    const int k2 = u >> glogL, l = u & (GL - 1);
-    cx p = make_cx(0.f, 0.f);
-    if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + x.n1 * k2)));
-    oth[ipos(k2, l, GL)] = p;
-  }
-}
-
-// store phase of every kind
-template <int T, int SIGN>
-AF_HD void item_end(int tid, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm,
-                    const cx* res, float& loss) {
-  const FSmem m = smem_of(S, sm);
+  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int n1 = x.n1, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn);
+    copy_tables(tid, T, S, m);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
+  ex.phase_sum([&](int tid, float& loss) {
+    for (int u = tid; u < L * GL; u += T) {
+      const int k2 = u >> glogR, l = u & (GL - 1);
+      if (l < cn) sk.put(x.off + c0 + l + (i64)n1 * k2, res[lpos(k2, l, S.LS)], loss);
+    }
+  });
+}
+
+// FK_BROWS (Bluestein pass R): lines k1 in [c0, c0 + cn), element j2 at
+// ws[j2 M1 + k1]; FFT_M2; times the spectrum at k1 + M1 k2 and conjugated;
+// FFT_M2 again; twiddle W_M^(j2 k1); stored line-contiguous in the
+// transform's second workspace region: ws[M + k1 M2 + j2] (other items of
+// this pass still read the first).
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogL = ilog2i(GL), c0 = it.c0, cn = it.cn;
-  switch (it.kind) {
-    case FK_DIRECT: {
-      DirectOut o{sk, xf};
-      final_any<SIGN>(tid, T, it.count, S, res, S.line.npass ? S.LS : 1, m.ftw, o, loss);
-      break;
+  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int M1 = x.n1, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn);
+    copy_multi_tables(tid, T, S, m, x);
+  });
+  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* nxt = res == m.a ? m.b : m.a;
+  ex.phase([&](int tid) {
+#pragma unroll 4
+    for (int u = tid; u < L * GL; u += T) {
+      const int k2 = u >> glogR, l = u & (GL - 1);
+      cx p = make_cx(0.f, 0.f);
+      if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + M1 * k2)));
+      nxt[ipos(k2, l, GL)] = p;
     }
-    case FK_BLUE: {
-      BlueOut<SIGN> o{sk, xf};
-      final_any<SIGN>(tid, T, it.count, S, res, S.line.npass ? S.LS : 1, m.ftw, o, loss);
-      break;
+  });
+  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  ex.phase([&](int tid) {
+    for (int u = tid; u < cn * L; u += T) {
+      const int l = (int)fdiv((unsigned)u, S.L1div);
+      const int j2 = u - l * L;
+      const int k1 = c0 + l;
+      A.ws[x.ws + x.M + (i64)k1 * L + j2] =
+          cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
     }
-    case FK_COLS:
-    case FK_BCOLS:
-      for (int u = tid; u < cn * L; u += T) {
-        const int c = (int)fdiv((unsigned)u, S.L1div);
-        const int k1 = u - c * L;
-        const int j2 = c0 + c;
-        A.ws[x.ws + (i64)j2 * L + k1] = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-      }
-      break;
-    case FK_ROWS:
-      for (int u = tid; u < L * GL; u += T) {
-        const int k2 = u >> glogL, l = u & (GL - 1);
-        if (l < cn) sk.put(x.off + c0 + l + (i64)x.n1 * k2, res[lpos(k2, l, S.LS)], loss);
-      }
-      break;
-    case FK_BROWS:
-      for (int u = tid; u < cn * L; u += T) {
-        const int l = (int)fdiv((unsigned)u, S.L1div);
-        const int j2 = u - l * L;
-        const int k1 = c0 + l;
-        A.ws[x.ws + x.M + (i64)k1 * L + j2] =
-            cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-      }
-      break;
-    default:  // FK_BCOLS2
-      for (int u = tid; u < L * GL; u += T) {
-        const int j1 = u >> glogL, c = u & (GL - 1);
-        const int j = j1 * x.n2 + c0 + c;
-        if (c < cn && j < x.n)
-          sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
-      }
-      break;
-  }
+  });
+}
+
+// FK_BCOLS2 (Bluestein pass A'): columns j2 in [c0, c0 + cn), element k1 at
+// ws[M + k1 M2 + j2]; FFT_M1; y_m = a_m (.) conj(.) at m = j1 M2 + j2 < n.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = xf[0];
+  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int M2 = x.n2, c0 = it.c0, cn = it.cn;
+  ex.phase_async([&](int tid) {
+    load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn);
+    copy_multi_tables(tid, T, S, m, x);
+  });
+  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const Sink sk{A.out, A.w};
+  ex.phase_sum([&](int tid, float& loss) {
+    for (int u = tid; u < L * GL; u += T) {
+      const int j1 = u >> glogC, c = u & (GL - 1);
+      const int j = j1 * M2 + c0 + c;
+      if (c < cn && j < x.n)
+        sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
+    }
+  });
 }
 
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
 AF_HD void run_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
-  ex.phase_async([&](int tid) { item_load<T, SIGN>(tid, A, it, S, xf, sm); });
-  if (it.kind == FK_BCOLS) ex.phase([&](int tid) { item_chirp_in<T, SIGN>(tid, it, S, xf, sm); });
-  const int nfft = (it.kind == FK_BLUE || it.kind == FK_BROWS) ? 2 : 1;
-  cx* src = sm;
-  cx* dst = sm + S.cap;
-  for (int f = 0; f < nfft; ++f) {
-    cx* res = line_fft<T, SIGN>(ex, S, src, dst, sm + 2 * S.cap);
-    cx* oth = res == sm ? sm + S.cap : sm;
-    if (f + 1 < nfft) {
-      ex.phase_sum([&](int tid, float& loss) { item_mid<T, SIGN>(tid, it, S, xf, sm, res, oth, loss); });
-      src = oth;
-      dst = res;
-    } else {
-      ex.phase_sum([&](int tid, float& loss) { item_end<T, SIGN>(tid, A, it, S, xf, sm, res, loss); });
-    }
+  switch (it.kind) {
+    case FK_BLUE: blue_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_COLS: cols_item<T, SIGN>(ex, A, it, S, xf, sm, false); break;
+    case FK_BCOLS: cols_item<T, SIGN>(ex, A, it, S, xf, sm, true); break;
+    case FK_ROWS: rows_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_BROWS: brows_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    case FK_BCOLS2: bcols2_item<T, SIGN>(ex, A, it, S, xf, sm); break;
+    default: direct_item<T, SIGN>(ex, A, it, S, xf, sm); break;
   }
 }
+
 // CTAs per SM the register budget allows for: 6 x 128, 3 x 256, 1 x 512 threads
 #define AFF_MINB(T) ((T) <= 128 ? 6 : ((T) <= 256 ? 3 : 1))
 

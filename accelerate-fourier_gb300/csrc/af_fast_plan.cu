@@ -27,9 +27,9 @@ static i64 even_up(i64 v) { return (v + 1) & ~(i64)1; }
 
 // Planner choices the autotuner varies.
 struct FastTune {
-  int radix16 = 0;          // radix-16 passes where the length allows (else radix 8)
-  int gl_max = 16;          // most lines in one multi-pass item
-  int balance_v = 1;        // per-pass choice of lines per unit (else two whenever possible)
+  int radix16 = 1;          // radix-16 passes where the length allows (else radix 8)
+  int gl_max = 32;          // most lines in one multi-pass item
+  int balance_v = 0;        // per-pass choice of lines per unit (else two whenever possible)
   int target = 4096;        // elements one item aims at
 };
 
