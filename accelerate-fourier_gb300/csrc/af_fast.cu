@@ -332,12 +332,17 @@ AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
 }
 
 // Lines [0, cn) of a strided matrix, rows e < L, into the interleaved layout
-// dst[e GL + c] = src[e stride + c] (lines cn..GL-1 zero).  Pairs of lines move
-// as 16-byte copies at L2 when every pair is 16-byte aligned; otherwise one
-// element at a time, at L2 for workspace sources (WS: written by other CTAs
-// of this launch, so never read through L1).
+// dst[e GL + c] = src[e stride + c]; lines cn..GL-1, and source positions
+// e stride + c >= lim, read as zero.  Pairs of lines move as 16-byte copies
+// at L2 when every pair is 16-byte aligned; otherwise one element at a time,
+// at L2 for workspace sources (WS: written by other CTAs of this launch, so
+// never read through L1).
+// no limit on the source positions
+#define kAll ((i64)1 << 62)
 template <bool WS>
-AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn) {
+AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn,
+                      i64 lim) {
+  const cx z = make_cx(0.f, 0.f);
   const bool v16 = GL >= 2 && ((reinterpret_cast<unsigned long long>(src) & 15) == 0) && (stride % 2 == 0) &&
                    (cn % 2 == 0);
   if (v16) {
@@ -345,19 +350,25 @@ AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, 
     for (int i = tid; i < L * half; i += T) {
       const int e = i >> hlog, c = (i & (half - 1)) * 2;
       cx* d = dst + e * GL + c;
-      if (c < cn) {
-        cp_async16(d, src + e * stride + c);
+      const i64 s = e * stride + c;
+      if (c < cn && s + 1 < lim) {
+        cp_async16(d, src + s);
+      } else if (c < cn && s < lim) {
+        if (WS) d[0] = ldws(src + s);
+        else cp_async8(d, src + s);
+        d[1] = z;
       } else {
-        d[0] = make_cx(0.f, 0.f);
-        d[1] = make_cx(0.f, 0.f);
+        d[0] = z;
+        d[1] = z;
       }
     }
   } else {
     for (int i = tid; i < L * GL; i += T) {
       const int e = i >> glog, c = i & (GL - 1);
-      if (c >= cn) dst[i] = make_cx(0.f, 0.f);
-      else if (WS) dst[i] = ldws(src + e * stride + c);
-      else cp_async8(dst + i, src + e * stride + c);
+      const i64 s = e * stride + c;
+      if (c >= cn || s >= lim) dst[i] = z;
+      else if (WS) dst[i] = ldws(src + s);
+      else cp_async8(dst + i, src + s);
     }
   }
 }
@@ -484,18 +495,19 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
   const int n2 = x.n2, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    if (!blue) {
-      load_lines<false>(tid, T, m.a, GL, glogC, A.in + x.off + c0, n2, L, cn);
-    } else {
-      for (int i = tid; i < L * GL; i += T) {
-        const int e = i >> glogC, c = i & (GL - 1);
-        const int j = e * n2 + c0 + c;  // natural index of element e of column c0 + c
-        m.a[i] = c < cn && j < x.n ? cmul_s<SIGN>(ldcx(A.in + x.off + j), chirp_at<true>(x, x.ct, j))
-                                   : make_cx(0.f, 0.f);
-      }
-    }
+    // FK_BCOLS: x zero padded past n (natural index j = e n2 + c0 + c)
+    load_lines<false>(tid, T, m.a, GL, glogC, A.in + x.off + c0, n2, L, cn, blue ? (i64)x.n - c0 : kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
+  if (blue) {  // the chirp a_j on the loaded x_j, from the staged table
+    ex.phase([&](int tid) {
+      for (int i = tid; i < L * GL; i += T) {
+        const int e = i >> glogC, c = i & (GL - 1);
+        const int j = e * n2 + c0 + c;
+        if (c < cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
+      }
+    });
+  }
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
@@ -518,7 +530,7 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int n1 = x.n1, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn);
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn, kAll);
     copy_tables(tid, T, S, m);
   });
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
@@ -544,18 +556,30 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int M1 = x.n1, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn);
+    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn, kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
   cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   ex.phase([&](int tid) {
-#pragma unroll 4
-    for (int u = tid; u < L * GL; u += T) {
-      const int k2 = u >> glogR, l = u & (GL - 1);
-      cx p = make_cx(0.f, 0.f);
-      if (l < cn) p = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], spec_at(x.spec, x.M, c0 + l + M1 * k2)));
-      nxt[ipos(k2, l, GL)] = p;
+    // four spectrum loads in flight per thread before their products
+    const int tot = L * GL;
+    for (int u0 = tid; u0 < tot; u0 += 4 * T) {
+      cx sp[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int u = u0 + r * T;
+        const int k2 = u >> glogR, l = u & (GL - 1);
+        sp[r] = (u < tot && l < cn) ? spec_at(x.spec, x.M, c0 + l + M1 * k2) : make_cx(0.f, 0.f);
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int u = u0 + r * T;
+        if (u < tot) {
+          const int k2 = u >> glogR, l = u & (GL - 1);
+          nxt[ipos(k2, l, GL)] = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], sp[r]));
+        }
+      }
     }
   });
   res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
@@ -580,7 +604,7 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
   const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
   const int M2 = x.n2, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn);
+    load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn, kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
   const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
