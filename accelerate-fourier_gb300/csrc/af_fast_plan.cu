@@ -31,6 +31,8 @@ struct FastTune {
   int gl_max = 32;          // most lines in one multi-pass item
   int balance_v = 0;        // per-pass choice of lines per unit (else two whenever possible)
   int target = 4096;        // elements one item aims at
+  int slack = 456;          // items queued between dependent stages (about the resident CTAs)
+  int l2_mb = 48;           // workspace in flight, MB (kept well inside the 126 MB L2)
 };
 
 // Radices of a 5-smooth line length: 16s or 8s first (the first pass has no
@@ -106,8 +108,6 @@ struct FastBatch {
   std::vector<FItem> queue;  // the persistent launch's items, in order
   int nctrs = FC_FIRST;
   size_t smem = 0;
-  int slack = 456;                  // items between dependent stages (about the resident CTAs)
-  i64 l2_budget = (i64)6 << 20;     // workspace elements in flight (48 MB)
   unsigned* dctrs = nullptr;
   int grid = 0;
   long long spin_limit = 1ll << 20; // polls before a wait gives up (under a second)
@@ -473,7 +473,7 @@ static void plan_batch(FastBatch* B) {
   for (int t : four) passes(t, false);
   for (int t : blue3) passes(t, true);
   B->smem = kCtaSmem;
-  order_queue(B, multi, singles, B->slack, B->l2_budget);
+  order_queue(B, multi, singles, B->tune.slack, (i64)B->tune.l2_mb << 17);
 }
 
 // ------------------------------------------------------------ spectra
@@ -634,12 +634,14 @@ FastBatch* fast_create(const i64* ns, i64 count, bool emu, const int* tune, int 
   try {
     B->emu = emu;
     // tuning overrides in FastTune field order; a negative entry keeps the default
-    int* fields[] = {&B->tune.radix16, &B->tune.gl_max, &B->tune.balance_v, &B->tune.target};
-    for (int i = 0; i < ntune && i < 4; ++i)
+    int* fields[] = {&B->tune.radix16, &B->tune.gl_max, &B->tune.balance_v, &B->tune.target, &B->tune.slack,
+                     &B->tune.l2_mb};
+    for (int i = 0; i < ntune && i < 6; ++i)
       if (tune[i] >= 0) *fields[i] = tune[i];
     if (B->tune.gl_max < 2 || B->tune.gl_max > 128 || (B->tune.gl_max & (B->tune.gl_max - 1)))
       throw FastError("lines per item must be a power of two in [2, 128]");
     if (B->tune.target < 256 || B->tune.target > 8192) throw FastError("item target must be in [256, 8192]");
+    if (B->tune.l2_mb < 1 || B->tune.l2_mb > 4096) throw FastError("workspace budget must be in [1, 4096] MB");
     B->ns.assign(ns, ns + count);
     B->offs.resize(count);
     i64 o = 0;
