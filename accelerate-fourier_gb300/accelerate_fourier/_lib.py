@@ -67,6 +67,7 @@ SIGNATURES = {
     "af_batch_exec": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_vjp": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_forward_cotangent": ([PTR, PTR, PTR, PTR, PTR, PTR], INT),
+    "af_batch_status": ([PTR, PTR], INT),
     "af_exec_c2c_noalloc": ([I64, INT, PTR, PTR, I64, PTR], INT),
     "af_cyclic_reverse_2d": ([INT, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
     "af_exec_c2c_axis": ([PTR, INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
@@ -213,6 +214,11 @@ class Batch:
 
     def forward_cotangent_ptr(self, x, w, cot, loss, stream=0):
         check(load().af_batch_forward_cotangent(self._h, x, w, cot, loss, stream))
+
+    def status(self, stream=0):
+        """Waits for the last call on `stream`; raises AfError (AF_ERR_TIMEOUT)
+        when a work item of its persistent launch gave up waiting."""
+        check(load().af_batch_status(self._h, stream))
 
     def __del__(self):
         try:

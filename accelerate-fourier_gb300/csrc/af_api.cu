@@ -10,11 +10,27 @@ namespace af {
 cudaError_t batch_run(BatchPlan* B, bool inverse, const float2* in, float2* out, const float* w, double* loss,
                       cudaStream_t st);
 i64 batch_launches(BatchPlan* B);
+// the persistent executor (af_fast_plan.cu)
+struct FastBatch;
+FastBatch* fast_create(const i64* ns, i64 count, bool emu, const int* tune, int ntune);
+void fast_destroy(FastBatch* B);
+cudaError_t fast_exec(FastBatch* B, int sign, const float2* in, float2* out, const float* w, double* loss,
+                      cudaStream_t st);
+int fast_status(FastBatch* B, cudaStream_t st);
+bool fast_supports(const i64* ns, i64 count);
+bool fast_poison_wait(FastBatch* B, long long spin_limit);
 }  // namespace af
 
+// A batch runs on the persistent executor (one launch per call) when every
+// length fits its tables; otherwise on the multi-launch batch plan.
 struct af_batch_s {
+  af::FastBatch* f = nullptr;
   af::BatchPlan* b = nullptr;
-  ~af_batch_s() { af::batch_destroy(b); }
+  int sign = -1;
+  ~af_batch_s() {
+    af::fast_destroy(f);
+    af::batch_destroy(b);
+  }
 };
 
 static thread_local std::string g_err;
@@ -116,8 +132,10 @@ af_status af_batch_create(af_batch* batch, const int64_t* lengths, int64_t count
   if (count < 0) return fail(AF_ERR_INVALID, "negative count");
   if (sign != 1 && sign != -1) return fail(AF_ERR_INVALID, "sign must be -1 or +1");
   af_batch_s* B = new af_batch_s();
+  B->sign = sign;
   try {
-    B->b = batch_create((const i64*)lengths, count, sign);
+    if (fast_supports((const i64*)lengths, count)) B->f = fast_create((const i64*)lengths, count, false, nullptr, 0);
+    else B->b = batch_create((const i64*)lengths, count, sign);
   } catch (...) {
     delete B;
     throw;
@@ -137,7 +155,7 @@ af_status af_batch_destroy(af_batch batch) {
 af_status af_batch_launches(af_batch batch, int64_t* launches) {
   AF_TRY
   if (!batch || !launches) return fail(AF_ERR_INVALID, "null argument");
-  *launches = batch_launches(batch->b);
+  *launches = batch->f ? 1 : batch_launches(batch->b);
   return AF_OK;
   AF_CATCH
 }
@@ -149,8 +167,26 @@ static af_status batch_exec_impl(af_batch batch, bool inverse, const float* in, 
   if (((uintptr_t)in | (uintptr_t)out) & 7) return fail(AF_ERR_INVALID, "data must be 8-byte aligned");
   if (w && !loss) return fail(AF_ERR_INVALID, "the cotangent epilogue needs a loss accumulator");
   if (loss) check_cuda(cudaMemsetAsync(loss, 0, sizeof(double), (cudaStream_t)stream), "loss reset");
-  check_cuda(batch_run(batch->b, inverse, (const float2*)in, (float2*)out, w, loss, (cudaStream_t)stream),
-             "batch launch");
+  if (batch->f)
+    check_cuda(fast_exec(batch->f, inverse ? -batch->sign : batch->sign, (const float2*)in, (float2*)out, w, loss,
+                         (cudaStream_t)stream),
+               "batch launch");
+  else
+    check_cuda(batch_run(batch->b, inverse, (const float2*)in, (float2*)out, w, loss, (cudaStream_t)stream),
+               "batch launch");
+  return AF_OK;
+  AF_CATCH
+}
+
+af_status af_batch_status(af_batch batch, af_stream stream) {
+  AF_TRY
+  if (!batch) return fail(AF_ERR_INVALID, "null argument");
+  if (!batch->f) {
+    check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch status");
+    return AF_OK;
+  }
+  if (fast_status(batch->f, (cudaStream_t)stream) != 0)
+    return fail(AF_ERR_TIMEOUT, "a work item of the last batch call waited too long for its previous stage");
   return AF_OK;
   AF_CATCH
 }
@@ -170,3 +206,15 @@ af_status af_batch_forward_cotangent(af_batch batch, const float* x, const float
 }
 
 }  // extern "C"
+
+// Test hook of the timeout path (internal, used by the GPU tests): see
+// fast_poison_wait.  Returns 0 when the batch's next call will time out.
+extern "C" __attribute__((visibility("default"))) int afx_batch_poison_wait(af_batch batch, long long spin_limit) {
+  try {
+    if (!batch || !batch->f) return 1;
+    return af::fast_poison_wait(batch->f, spin_limit) ? 0 : 1;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}

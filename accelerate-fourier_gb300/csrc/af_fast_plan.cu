@@ -629,6 +629,27 @@ static void bind_batch(FastBatch* B, cudaStream_t st) {
   fcheck(cudaStreamSynchronize(st), "batch upload");
 }
 
+// Whether the executor plans every length: 5-smooth lengths that fit one CTA
+// or split into two factors of at most 1024; other lengths whose Bluestein
+// convolution length does the same, with 2n within the three-level tables.
+bool fast_supports(const i64* ns, i64 count) {
+  i64 total = 0;
+  for (i64 i = 0; i < count; ++i) {
+    const i64 n = ns[i];
+    if (n < 0) return false;
+    total += n;
+    if (n == 0) continue;
+    if (is_5smooth(n)) {
+      if (full_smem(n, 1, true) > kMaxSmem && (n > ((i64)1 << 18) || !four_step_n1(n))) return false;
+    } else {
+      const i64 M = blue_len(n);
+      if (2 * n > ((i64)1 << 18)) return false;
+      if (full_smem(M, 1, true) > kMaxSmem && (M > ((i64)1 << 18) || !four_step_n1(M))) return false;
+    }
+  }
+  return total < ((i64)1 << 31);
+}
+
 FastBatch* fast_create(const i64* ns, i64 count, bool emu, const int* tune, int ntune) {
   FastBatch* B = new FastBatch();
   try {
@@ -685,6 +706,23 @@ cudaError_t fast_exec(FastBatch* B, int sign, const cx* in, cx* out, const float
   cudaError_t e = cudaMemsetAsync(B->dctrs, 0, sizeof(unsigned) * B->nctrs, st);
   if (e != cudaSuccess) return e;
   return launch_fast(kThreads, sign, A, (int)B->hitems.size(), B->smem, B->dctrs, B->grid, B->spin_limit, st);
+}
+
+// Test hook: the first item of the queue that waits for a previous stage now
+// waits for one completion more than that stage makes, and every wait polls
+// at most `spin_limit` times, so the next launch ends with FE_TIMEOUT after a
+// bounded wait.  Returns false when no item waits.
+bool fast_poison_wait(FastBatch* B, long long spin_limit) {
+  for (size_t i = 0; i < B->hitems.size(); ++i) {
+    if (B->hitems[i].wait_ctr < 0) continue;
+    B->hitems[i].wait_cnt += 1;
+    B->queue[i].wait_cnt += 1;
+    B->spin_limit = spin_limit;
+    if (!B->emu)
+      fcheck(cudaMemcpy(B->ditems + i, &B->hitems[i], sizeof(FItem), cudaMemcpyHostToDevice), "items");
+    return true;
+  }
+  return false;
 }
 
 // FE_OK or FE_TIMEOUT of the last launch (waits for it to finish)
@@ -776,6 +814,15 @@ extern "C" __attribute__((visibility("default"))) int afx_fast_ws(void* b, float
   if (!B->emu || count > (int64_t)B->hws.size()) return 1;
   memcpy(out, B->hws.data(), sizeof(float2) * count);
   return 0;
+}
+
+extern "C" __attribute__((visibility("default"))) int afx_fast_poison_wait(void* b, long long spin_limit) {
+  try {
+    return af::fast_poison_wait((af::FastBatch*)b, spin_limit) ? 0 : 1;
+  } catch (const std::exception& e) {
+    g_fast_err = e.what();
+    return -1;
+  }
 }
 
 extern "C" __attribute__((visibility("default"))) int afx_fast_status(void* b, void* stream) {

@@ -144,11 +144,16 @@ af_status af_cyclic_reverse_2d(af_layout layout, const float* in_re,
 /* Batches of mixed lengths ------------------------------------------------
  * `count` transforms of lengths lengths[0..count) stored back to back
  * (transform i starts at sum_{j<i} lengths[j]).  Each transform is planned
- * like Planned.transform (Planned.hs:103-106); all of them run in a few
- * launches: transforms that fit one CTA share launches, larger ones run their
- * fused multi-pass schemes grouped so that the workspace stays in L2.
- * Interleaved Complex Float32 only.  The reference applies `transform` per
- * array; this entry point is the batched form of that call. */
+ * like Planned.transform (Planned.hs:103-106) computes it; every call is one
+ * persistent launch whose CTAs take work items from a queue: whole transforms
+ * of one CTA, and the stages of the two-pass four-step and three-pass
+ * Bluestein schemes of longer ones (a stage's items start once the previous
+ * stage's items have finished, through device counters with bounded waits;
+ * the workspace stays in L2).  Batches with a Bluestein length above 131072,
+ * or a 5-smooth length without a split into two factors of at most 1024,
+ * run on a multi-launch plan instead.  Interleaved Complex Float32 only; one
+ * call of a batch at a time.  The reference applies `transform` per array;
+ * this entry point is the batched form of that call. */
 typedef struct af_batch_s* af_batch;
 af_status af_batch_create(af_batch* batch, const int64_t* lengths, int64_t count, int sign);
 af_status af_batch_destroy(af_batch batch);
@@ -157,6 +162,12 @@ af_status af_batch_launches(af_batch batch, int64_t* launches);
 af_status af_batch_exec(af_batch batch, const float* in, float* out, af_stream stream);
 /* grad = DFT^H cot for every transform (the VJP of af_batch_exec). */
 af_status af_batch_vjp(af_batch batch, const float* cot, float* grad, af_stream stream);
+/* Waits for the batch's last call on `stream` and reports whether its
+ * persistent launch completed: AF_ERR_TIMEOUT when a work item gave up its
+ * bounded wait for the items of its previous stage (the outputs are then
+ * incomplete).  No counterpart in the reference, whose transforms run to
+ * completion inside `run`. */
+af_status af_batch_status(af_batch batch, af_stream stream);
 /* Forward transform with the spectral-weight epilogue of the loss
  * L = sum_i sum_k w_ik |X_ik|^2: writes cot = dL/dconj(X) * 2 = 2 w X and sets
  * *loss (device double) to L.  w holds one real weight per output element. */

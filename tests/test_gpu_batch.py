@@ -111,7 +111,7 @@ def test_benchmark_workload_sample():
     import bench
     sizes = bench.workload_sizes()
     b = make_batch(sizes, -1)
-    assert b.launches() <= 160
+    assert b.launches() == 1  # one persistent launch per call
     rng = np.random.default_rng(5)
     x = crand(rng, int(sizes.sum()), "normal")
     y = run(b, x)
@@ -124,3 +124,53 @@ def test_benchmark_workload_sample():
         worst = max(worst, err)
         assert err <= fp32_bound(n, 4.0), (n, err)
     assert worst < 1e-6
+
+
+def test_batch_in_place():
+    sizes = np.array([64, 1000, 4099, 20000, 30011], dtype=np.int64)
+    rng = np.random.default_rng(15)
+    x = crand(rng, int(sizes.sum()), "normal")
+    b = make_batch(sizes, -1)
+    xd = torch.from_numpy(x.astype(np.complex64)).cuda()
+    b.exec_ptr(xd.data_ptr(), xd.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    b.status(torch.cuda.current_stream().cuda_stream)
+    y = xd.cpu().numpy()
+    for n, xi, yi in zip(sizes, split(x, sizes), split(y, sizes)):
+        assert rel_l2(yi, O().planned(xi[None], -1)[0]) <= fp32_bound(n, 4.0), int(n)
+
+
+def test_lengths_beyond_the_executor_use_the_multi_launch_plan():
+    """A Bluestein length above 131072 runs on the multi-launch batch plan."""
+    sizes = np.array([200003, 64], dtype=np.int64)
+    rng = np.random.default_rng(16)
+    x = crand(rng, int(sizes.sum()), "normal")
+    b = make_batch(sizes, -1)
+    assert b.launches() > 1
+    y = run(b, x)
+    for n, xi, yi in zip(sizes, split(x, sizes), split(y, sizes)):
+        assert rel_l2(yi, O().planned(xi[None], -1)[0]) <= fp32_bound(n, 4.0), int(n)
+
+
+def test_stage_wait_timeout_is_reported_and_the_device_stays_usable():
+    """A work item whose previous stage never reaches its count gives up after
+    a bounded number of polls: the launch ends, af_batch_status reports
+    AF_ERR_TIMEOUT, and the next batch runs normally."""
+    import ctypes
+    from accelerate_fourier import _lib
+    sizes = np.array([30011, 20000, 64], dtype=np.int64)
+    b = make_batch(sizes, -1)
+    L = _lib.load()
+    L.afx_batch_poison_wait.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
+    assert L.afx_batch_poison_wait(b._h, 20000) == 0
+    x = torch.ones(int(sizes.sum()), dtype=torch.complex64, device="cuda")
+    y = torch.empty_like(x)
+    s = torch.cuda.current_stream().cuda_stream
+    b.exec_ptr(x.data_ptr(), y.data_ptr(), s)
+    with pytest.raises(_lib.AfError) as e:
+        b.status(s)
+    assert e.value.code == 5  # AF_ERR_TIMEOUT
+    rng = np.random.default_rng(17)
+    xs = crand(rng, int(sizes.sum()), "normal")
+    ys = run(make_batch(sizes, -1), xs)
+    for n, xi, yi in zip(sizes, split(xs, sizes), split(ys, sizes)):
+        assert rel_l2(yi, O().planned(xi[None], -1)[0]) <= fp32_bound(n, 4.0), int(n)
