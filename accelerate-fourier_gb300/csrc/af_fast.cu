@@ -276,6 +276,17 @@ AF_HD void final_any(int tid, int T, int cnt, const FShape& S, const cx* src, in
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
 AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
+  if (S.fixed) {  // a compile-time line (the planner sets `fixed` only for listed pairs)
+    switch (S.line.L * 1024 + S.GL) {
+#define AFF_FIXED_CASE(L, GL)                              \
+  case L * 1024 + GL:                                      \
+    cline_passes<T, SIGN, L, GL, 0>(ex, src, dst, tw);     \
+    return src;
+      AFF_FIXED_LINES(AFF_FIXED_CASE)
+#undef AFF_FIXED_CASE
+      default: break;
+    }
+  }
   const int np = S.line.npass;
   for (int j = 0; j < np; ++j) {
     const FPass ps = S.line.pass[j];
@@ -289,6 +300,37 @@ AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
     dst = t;
   }
   return src;
+}
+
+// The kernel's shared memory: the dynamic area of the items, and the staged
+// descriptors of the current item (namespace scope, so that the out-of-line
+// line FFT addresses them as shared memory).
+#ifdef __CUDACC__
+extern __shared__ float4 fsm4[];
+__shared__ FShape s_shape;
+__shared__ FXform s_xf[AFF_MAXQ];
+__shared__ FItem s_it;
+__shared__ int s_item, s_ok;
+
+// One out-of-line copy of the line FFT per sign, shared by every item kind
+// (keeps the kernel's code, and its compile time, small); its buffers are
+// element offsets into the dynamic shared area.
+template <int T, int SIGN>
+__device__ __noinline__ int line_fft_dev(int so, int doff, int toff) {
+  DevExec ex;
+  cx* base = reinterpret_cast<cx*>(fsm4);
+  cx* r = line_fft<T, SIGN>(ex, s_shape, base + so, base + doff, base + toff);
+  return (int)(r - base);
+}
+template <int T, int SIGN>
+__device__ __forceinline__ cx* run_line(DevExec&, const FShape&, cx* sm, cx* src, cx* dst, const cx* tw) {
+  return sm + line_fft_dev<T, SIGN>((int)(src - sm), (int)(dst - sm), (int)(tw - sm));
+}
+#endif
+// the emulator runs the line FFT inline
+template <int T, int SIGN>
+cx* run_line(HostExec& ex, const FShape& S, cx*, cx* src, cx* dst, const cx* tw) {
+  return line_fft<T, SIGN>(ex, S, src, dst, tw);
 }
 
 // shared-memory areas of an item: the two data buffers, the pass twiddles,
@@ -403,7 +445,7 @@ AF_HD void direct_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
     }
     copy_tables(tid, T, S, m);
   });
-  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const int LS = S.line.npass ? S.LS : 1;  // no pass: the load layout read as line-major with LS 1
   DirectOut f{Sink{A.out, A.w}, xf};
   ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, f, loss); });
@@ -458,7 +500,7 @@ AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
     copy_tables(tid, T, S, m);
   });
   const int LS = S.line.npass ? S.LS : 1;
-  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   BlueMidS<SIGN> mid;
   mid.xf = xf;
@@ -469,7 +511,7 @@ AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   mid.G = G;
   mid.GL = GL;
   ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, Q, S, res, LS, m.ftw, mid, loss); });
-  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  res = run_line<T, SIGN>(ex, S, sm, nxt, res, m.tw);
   BlueOut<SIGN> out{Sink{A.out, A.w}, xf};
   ex.phase_sum([&](int tid, float& loss) { final_any<SIGN>(tid, T, cnt, S, res, LS, m.ftw, out, loss); });
 }
@@ -508,7 +550,7 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
       }
     });
   }
-  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int c = (int)fdiv((unsigned)u, S.L1div);
@@ -533,7 +575,7 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
     load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn, kAll);
     copy_tables(tid, T, S, m);
   });
-  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
     for (int u = tid; u < L * GL; u += T) {
@@ -559,7 +601,7 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
     load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn, kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
-  cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   ex.phase([&](int tid) {
     // four spectrum loads in flight per thread before their products
@@ -582,7 +624,7 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
       }
     }
   });
-  res = line_fft<T, SIGN>(ex, S, nxt, res, m.tw);
+  res = run_line<T, SIGN>(ex, S, sm, nxt, res, m.tw);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int l = (int)fdiv((unsigned)u, S.L1div);
@@ -607,7 +649,7 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
     load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn, kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
-  const cx* res = line_fft<T, SIGN>(ex, S, m.a, m.b, m.tw);
+  const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
     for (int u = tid; u < L * GL; u += T) {
@@ -661,11 +703,6 @@ __device__ __forceinline__ void copy_words(void* dst, const void* src, int n) {
 template <int T, int SIGN>
 __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitems, unsigned* ctrs,
                                                               long long spin_limit) {
-  extern __shared__ float4 fsm4[];
-  __shared__ FShape s_shape;
-  __shared__ FXform s_xf[AFF_MAXQ];
-  __shared__ FItem s_it;
-  __shared__ int s_item, s_ok;
   DevExec ex;
   int loaded = -1;  // shape staged in s_shape (uniform across the CTA)
   int next = 0;     // thread 0: the item claimed for the next round

@@ -173,6 +173,114 @@ AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, in
   }
 }
 
+// ------------------------------------------------------------ compile-time lines
+// A line FFT whose length L and line count GL are template constants runs
+// the passes the planner makes for it (radix 16s, 8s, 5s, one 4, 3s, 2s;
+// two lines per unit except at radix 16; m-major twiddles at the same table
+// offsets), with every stride, loop bound and divisor known to the compiler.
+// AFF_FIXED_LINES lists the (L, GL) pairs compiled this way.
+#define AFF_FIXED_LINES(X)                                                                                   \
+  X(128, 16) X(160, 16) X(192, 16) X(200, 16) X(240, 16) X(250, 16) X(256, 16) X(288, 8) X(300, 8) X(320, 8) \
+  X(360, 8) X(384, 8)
+
+struct CRadices {
+  int n;
+  int r[AFF_MAXPASS];
+};
+constexpr CRadices c_radices(int L) {
+  CRadices x{0, {}};
+  int m = L;
+  while (m % 16 == 0) { x.r[x.n++] = 16; m /= 16; }
+  while (m % 8 == 0) { x.r[x.n++] = 8; m /= 8; }
+  while (m % 5 == 0) { x.r[x.n++] = 5; m /= 5; }
+  if (m % 4 == 0) { x.r[x.n++] = 4; m /= 4; }
+  while (m % 3 == 0) { x.r[x.n++] = 3; m /= 3; }
+  while (m % 2 == 0) { x.r[x.n++] = 2; m /= 2; }
+  return x;
+}
+// span of the butterflies before pass j
+constexpr int c_span(int L, int j) {
+  int p = 1;
+  for (int i = 0; i < j; ++i) p *= c_radices(L).r[i];
+  return p;
+}
+// twiddle-table offset of pass j (each pass after the first: p (R-1) entries, even)
+constexpr int c_twoff(int L, int j) {
+  int t = 0;
+  for (int i = 0; i < j; ++i) {
+    const int p = c_span(L, i);
+    if (p > 1) t += (p * (c_radices(L).r[i] - 1) + 1) & ~1;
+  }
+  return t;
+}
+
+// One unit of a compile-time pass (fpass_unit with constant P, NB, GL, LS).
+template <int R, int V, int SIGN, int P, int NB, int GL, int LS>
+AF_HD void cpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, int b, int line, const cx* __restrict__ tw) {
+  cx a[V][R];
+  const int ib = b * GL + line;
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    cx t[V];
+    FVec<V>::get(src + ib + m * (NB * GL), t);
+#pragma unroll
+    for (int v = 0; v < V; ++v) a[v][m] = t[v];
+  }
+  const int q = b / P;
+  const int k = b - q * P;
+  if (P > 1 && k > 0) {
+    cx w[R];
+    pass_twiddles<R>(tw, k, P, w);
+#pragma unroll
+    for (int m = 1; m < R; ++m)
+#pragma unroll
+      for (int v = 0; v < V; ++v) a[v][m] = cmul_s<SIGN>(a[v][m], w[m]);
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) Dft<R>::run(a[v], (rl)SIGN, nullptr, 0, 0);
+  const int oe = q * P * R + k;
+  if (LS == 0) {
+    const int ob = oe * GL + line;
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      cx t[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) t[v] = a[v][m];
+      FVec<V>::put(dst + ob + m * (P * GL), t);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int m = 0; m < R; ++m) dst[(line + v) * LS + oe + m * P] = a[v][m];
+  }
+}
+
+template <int T, int R, int V, int SIGN, int P, int NB, int GL, int LS>
+AF_HD void cpass_thread(int tid, const cx* src, cx* dst, const cx* tw) {
+  constexpr int per = GL / V, units = NB * per;
+  for (int u = tid; u < units; u += T) cpass_unit<R, V, SIGN, P, NB, GL, LS>(src, dst, u / per, (u % per) * V, tw);
+}
+
+// Passes J.. of the compile-time line (L, GL); src and dst swap after each.
+#pragma nv_exec_check_disable
+template <int T, int SIGN, int L, int GL, int J, class E>
+AF_HD void cline_passes(E& ex, cx*& src, cx*& dst, const cx* tw) {
+  constexpr CRadices rs = c_radices(L);
+  if constexpr (J < rs.n) {
+    constexpr int R = rs.r[J], P = c_span(L, J), NB = L / R;
+    constexpr int V = (GL >= 2 && R != 16) ? 2 : 1;
+    constexpr int LSo = J == rs.n - 1 ? (L | 1) : 0;
+    constexpr int TW = c_twoff(L, J);
+    cx* s = src;
+    cx* d = dst;
+    ex.phase([&](int tid) { cpass_thread<T, R, V, SIGN, P, NB, GL, LSo>(tid, s, d, tw + TW); });
+    src = d;
+    dst = s;
+    cline_passes<T, SIGN, L, GL, J + 1>(ex, src, dst, tw);
+  }
+}
+
 // w^l for l < G from w (at most three products deep for G <= 16)
 template <int G>
 AF_HD void powers(cx w, cx* p) {

@@ -37,6 +37,7 @@ struct FShape {
   FLine line;
   int kind;
   int n, G, Q, GL, LS, cap, ftwn, aux;
+  int fixed;  // the line FFT is one of the compile-time lines (AFF_FIXED_LINES)
   int smem;  // shared-memory bytes an item of this shape uses
   FastDiv ndiv, L1div;
   const cx* tw;   // pass twiddles (line.twn entries)

@@ -31,9 +31,17 @@ struct FastTune {
   int gl_max = 32;          // most lines in one multi-pass item
   int balance_v = 0;        // per-pass choice of lines per unit (else two whenever possible)
   int target = 4096;        // elements one item aims at
-  int slack = 456;          // items queued between dependent stages (about the resident CTAs)
+  int slack = 1368;         // items queued between dependent stages (three times the resident CTAs)
   int l2_mb = 48;           // workspace in flight, MB (kept well inside the 126 MB L2)
+  int fixed = 1;            // compile-time line FFTs for the listed (L, GL) pairs
 };
+
+static bool is_fixed_line(int L, int GL) {
+#define AFF_FIXED_TEST(l, g) if (L == l && GL == g) return true;
+  AFF_FIXED_LINES(AFF_FIXED_TEST)
+#undef AFF_FIXED_TEST
+  return false;
+}
 
 // Radices of a 5-smooth line length: 16s or 8s first (the first pass has no
 // twiddles), then 5, 4, 3, 2.
@@ -182,6 +190,8 @@ static void choose_vectors(FShape& s, bool balance) {
 
 static void finish_shape(FShape& s, const FastTune& t) {
   choose_vectors(s, t.balance_v != 0);
+  // the compile-time passes are those of radix-16 lines with paired units
+  s.fixed = t.fixed && t.radix16 && !t.balance_v && s.kind < 0 && is_fixed_line(s.line.L, s.GL);
   s.LS = line_stride(s.line.L);
   s.cap = (int)even_up(std::max<i64>((i64)s.GL * s.line.L, (i64)s.GL * s.LS));
   s.aux = s.kind < 0 ? 1 : 0;
@@ -224,7 +234,8 @@ static int line_shape(FastBatch* B, int L) {
   // lines at most gl_max, GL * L at most the item target and within the
   // shared memory of a CTA (two buffers of GL line-major rows)
   int GL = B->tune.gl_max;
-  while (GL > 2 && ((i64)GL * L > B->tune.target || (i64)sizeof(cx) * 2 * GL * ((L | 1) + 1) > kMaxSmem * 7 / 8))
+  while (GL > 2 && ((i64)GL * L > B->tune.target ||
+                    (i64)sizeof(cx) * (2 * even_up((i64)GL * (L | 1)) + 2 * L + 2 * AFF_TL3 + 16) > kMaxSmem))
     GL /= 2;
   auto key = std::make_pair(L, GL);
   auto it = B->line_shapes.find(key);
@@ -656,8 +667,8 @@ FastBatch* fast_create(const i64* ns, i64 count, bool emu, const int* tune, int 
     B->emu = emu;
     // tuning overrides in FastTune field order; a negative entry keeps the default
     int* fields[] = {&B->tune.radix16, &B->tune.gl_max, &B->tune.balance_v, &B->tune.target, &B->tune.slack,
-                     &B->tune.l2_mb};
-    for (int i = 0; i < ntune && i < 6; ++i)
+                     &B->tune.l2_mb, &B->tune.fixed};
+    for (int i = 0; i < ntune && i < 7; ++i)
       if (tune[i] >= 0) *fields[i] = tune[i];
     if (B->tune.gl_max < 2 || B->tune.gl_max > 128 || (B->tune.gl_max & (B->tune.gl_max - 1)))
       throw FastError("lines per item must be a power of two in [2, 128]");
