@@ -179,9 +179,13 @@ AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, in
 // two lines per unit except at radix 16; m-major twiddles at the same table
 // offsets), with every stride, loop bound and divisor known to the compiler.
 // AFF_FIXED_LINES lists the (L, GL) pairs compiled this way.
-#define AFF_FIXED_LINES(X)                                                                                   \
-  X(128, 16) X(160, 16) X(192, 16) X(200, 16) X(240, 16) X(250, 16) X(256, 16) X(288, 8) X(300, 8) X(320, 8) \
-  X(360, 8) X(384, 8)
+// The lengths are those whose pairwise products serve as the Bluestein
+// convolution lengths of the multi-pass scheme; GL is the planner's line
+// count for each under the default tuning.
+#define AFF_FIXED_LINES(X)                                                                                     \
+  X(64, 32) X(80, 32) X(96, 32) X(100, 32) X(120, 32) X(128, 32) X(144, 16) X(160, 16) X(180, 16) X(192, 16) \
+  X(200, 16) X(216, 16) X(240, 16) X(250, 16) X(256, 16) X(270, 8) X(288, 8) X(300, 8) X(320, 8) X(360, 8)     \
+  X(384, 8) X(400, 8) X(432, 8) X(480, 8) X(500, 4) X(512, 4)
 
 struct CRadices {
   int n;

@@ -36,6 +36,55 @@ struct FastTune {
   int fixed = 1;            // compile-time line FFTs for the listed (L, GL) pairs
 };
 
+// The compile-time line lengths, and their pairwise products a b (a >= b)
+// in increasing order.
+static const std::vector<int>& fixed_lengths() {
+  static const std::vector<int> v = [] {
+    std::vector<int> r;
+#define AFF_FIXED_LEN(l, g) r.push_back(l);
+    AFF_FIXED_LINES(AFF_FIXED_LEN)
+#undef AFF_FIXED_LEN
+    return r;
+  }();
+  return v;
+}
+struct FixedProduct {
+  i64 M;
+  int a, b;
+};
+static const std::vector<FixedProduct>& fixed_products() {
+  static const std::vector<FixedProduct> v = [] {
+    std::vector<FixedProduct> r;
+    const std::vector<int>& L = fixed_lengths();
+    for (int a : L)
+      for (int b : L)
+        if (a >= b) r.push_back(FixedProduct{(i64)a * b, a, b});
+    std::sort(r.begin(), r.end(), [](const FixedProduct& x, const FixedProduct& y) {
+      return x.M != y.M ? x.M < y.M : (x.a - x.b) < (y.a - y.b);
+    });
+    return r;
+  }();
+  return v;
+}
+// the least product of two compiled lengths >= need (M = 0 when none)
+static FixedProduct least_fixed_product(i64 need) {
+  for (const FixedProduct& f : fixed_products())
+    if (f.M >= need) return f;
+  return FixedProduct{0, 0, 0};
+}
+// a split n = a b into compiled lengths, a >= b, the most balanced (M = 0 when none)
+static FixedProduct fixed_split(i64 n) {
+  FixedProduct best{0, 0, 0};
+  for (int b : fixed_lengths())
+    if (n % b == 0) {
+      const i64 a = n / b;
+      if (a < b) continue;
+      for (int l : fixed_lengths())
+        if (l == a && (!best.M || a - b < best.a - best.b)) best = FixedProduct{n, (int)a, b};
+    }
+  return best;
+}
+
 static bool is_fixed_line(int L, int GL) {
 #define AFF_FIXED_TEST(l, g) if (L == l && GL == g) return true;
   AFF_FIXED_LINES(AFF_FIXED_TEST)
@@ -380,19 +429,40 @@ static void order_queue(FastBatch* B, std::vector<MultiT>& multi, std::vector<FI
 static void plan_batch(FastBatch* B) {
   const bool r16 = B->tune.radix16 != 0;
   std::map<i64, std::vector<int>> direct_by_n, blue_by_M;
-  std::vector<int> four, blue3;
+  struct Split {
+    int t;
+    i64 N, n1, n2;
+  };
+  std::vector<Split> four, blue3;
   for (size_t i = 0; i < B->ns.size(); ++i) {
     const i64 n = B->ns[i];
     if (n == 0) continue;
     if (is_5smooth(n)) {
-      if (full_smem(n, 1, r16) <= kMaxSmem) direct_by_n[n].push_back((int)i);
-      else if (four_step_n1(n)) four.push_back((int)i);
-      else throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
+      if (full_smem(n, 1, r16) <= kMaxSmem) {
+        direct_by_n[n].push_back((int)i);
+      } else {  // four-step: a split into compiled line lengths when there is one
+        const FixedProduct f = B->tune.fixed ? fixed_split(n) : FixedProduct{0, 0, 0};
+        const i64 d = f.M ? f.b : four_step_n1(n);
+        if (!d) throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
+        four.push_back(Split{(int)i, n, d, n / d});
+      }
     } else {
       const i64 M = blue_len(n);
-      if (full_smem(M, 1, r16) <= kMaxSmem) blue_by_M[M].push_back((int)i);
-      else if (four_step_n1(M)) blue3.push_back((int)i);
-      else throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
+      if (full_smem(M, 1, r16) <= kMaxSmem) {
+        blue_by_M[M].push_back((int)i);
+        continue;
+      }
+      // multi-pass Bluestein: the least product of two compiled line lengths
+      // >= 2n - 1, the longer on the column passes (one FFT each), the
+      // shorter on the row pass (two FFTs)
+      const FixedProduct f = B->tune.fixed ? least_fixed_product(2 * n - 1) : FixedProduct{0, 0, 0};
+      if (f.M) {
+        blue3.push_back(Split{(int)i, f.M, f.a, f.b});
+      } else {
+        const i64 d = four_step_n1(M);
+        if (!d) throw FastError("length " + std::to_string(n) + " is too long for the batched executor");
+        blue3.push_back(Split{(int)i, M, d, M / d});
+      }
     }
   }
   std::vector<FItem> singles;
@@ -430,10 +500,10 @@ static void plan_batch(FastBatch* B) {
   for (auto& kv : blue_by_M) group_items(FK_BLUE, kv.first, kv.second);
   // multi-pass transforms: each owns a workspace region
   std::vector<MultiT> multi;
-  auto passes = [&](int t, bool blue) {
+  auto passes = [&](const Split& sp, bool blue) {
+    const int t = sp.t;
     const i64 n = B->ns[t];
-    const i64 N = blue ? blue_len(n) : n;  // length of the FFTs
-    const i64 n1 = four_step_n1(N), n2 = N / n1;
+    const i64 N = sp.N, n1 = sp.n1, n2 = sp.n2;  // length of the FFTs and its split
     FXform x = blank_xf(B->offs[t], n);
     x.n1 = (int)n1;
     x.n2 = (int)n2;
@@ -481,8 +551,8 @@ static void plan_batch(FastBatch* B) {
     }
     multi.push_back(std::move(mt));
   };
-  for (int t : four) passes(t, false);
-  for (int t : blue3) passes(t, true);
+  for (const Split& sp : four) passes(sp, false);
+  for (const Split& sp : blue3) passes(sp, true);
   B->smem = kCtaSmem;
   order_queue(B, multi, singles, B->tune.slack, (i64)B->tune.l2_mb << 17);
 }
@@ -653,9 +723,11 @@ bool fast_supports(const i64* ns, i64 count) {
     if (is_5smooth(n)) {
       if (full_smem(n, 1, true) > kMaxSmem && (n > ((i64)1 << 18) || !four_step_n1(n))) return false;
     } else {
+      if (2 * n > ((i64)1 << 18)) return false;  // the chirp's three-level table
       const i64 M = blue_len(n);
-      if (2 * n > ((i64)1 << 18)) return false;
-      if (full_smem(M, 1, true) > kMaxSmem && (M > ((i64)1 << 18) || !four_step_n1(M))) return false;
+      if (full_smem(M, 1, true) > kMaxSmem && !least_fixed_product(2 * n - 1).M &&
+          (M > ((i64)1 << 18) || !four_step_n1(M)))
+        return false;
     }
   }
   return total < ((i64)1 << 31);
@@ -748,10 +820,14 @@ int fast_status(FastBatch* B, cudaStream_t st) {
 std::string fast_describe(FastBatch* B) {
   std::ostringstream o;
   int kinds[8] = {0};
-  for (const FItem& it : B->queue) kinds[it.kind & 7]++;
+  i64 fixed = 0;
+  for (const FItem& it : B->queue) {
+    kinds[it.kind & 7]++;
+    fixed += B->shapes[it.shape].fixed;
+  }
   o << "{\"items\": " << B->queue.size() << ", \"grid\": " << B->grid << ", \"smem\": " << B->smem
     << ", \"counters\": " << B->nctrs << ", \"shapes\": " << B->shapes.size() << ", \"table_entries\": "
-    << B->tab_elems << ", \"ws_elems\": " << B->ws_elems << ", \"by_kind\": [";
+    << B->tab_elems << ", \"ws_elems\": " << B->ws_elems << ", \"fixed_items\": " << fixed << ", \"by_kind\": [";
   for (int k = 0; k < 7; ++k) o << (k ? ", " : "") << kinds[k];
   o << "]}";
   return o.str();
