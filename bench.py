@@ -34,7 +34,22 @@ for _p in (ROOT, os.path.join(ROOT, "accelerate-fourier_gb300")):
 METRIC = "C2C FFT GB/s & % HBM roofline (fwd+VJP, batched mixed N) vs plain; err vs FP64"
 UNIT = "GB/s"
 COUNT = 4096
-STEP_DRAM_BYTES = 2.667e9  # DRAM bytes per step of the default workload (ncu, see the profiles)
+TRAFFIC_PROFILE = os.path.join("profiles", "fast_kernel_workload_traffic.md")
+
+
+def profiled_traffic():
+    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one step's
+    persistent launches of the default workload, with the commit the ncu
+    capture was taken at, from the committed profile summary; None when the
+    summary is absent."""
+    import re
+    path = os.path.join(ROOT, TRAFFIC_PROFILE)
+    if not os.path.exists(path):
+        return None, None
+    txt = open(path).read()
+    m = re.search(r"traffic_bytes_per_step:\s*([0-9.e+]+)", txt)
+    c = re.search(r"profiled_at_commit:\s*([0-9a-f]+)", txt)
+    return (float(m.group(1)) if m else None), (c.group(1) if c else None)
 
 
 # ----------------------------------------------------------------- workload
@@ -192,27 +207,37 @@ def cpu_baseline(ns, budget_s: float = 12.0, threads: int = 0):
 
 # ----------------------------------------------------------------- GPU arm
 class PlainRunner:
-    """One plan per distinct length, one exec per transform (the plain
-    one-launch-per-size path)."""
+    """The plain one-launch-per-size GPU path: the same transforms laid out
+    grouped by length (one contiguous [count, n] block per distinct n), one
+    af_exec_c2c and one af_vjp_c2c per distinct length over its whole block,
+    and the cotangent g = 2 w X with the loss sum w |X|^2 as elementwise
+    device kernels.  The step is captured in a CUDA graph, so no host work
+    is timed."""
 
     def __init__(self, ns):
         from accelerate_fourier import _lib
-        self.ns = ns
-        self.offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
-        self.plans = {}
+        ns = np.asarray(ns, dtype=np.int64)
+        offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+        order = np.argsort(ns, kind="stable")
+        # gather index: grouped position -> natural position
+        self.gather = np.concatenate([np.arange(offs[i], offs[i] + ns[i]) for i in order]).astype(np.int64)
+        self.groups = []  # (plan, start element, count)
+        pos = 0
         for n in sorted(set(int(v) for v in ns)):
-            self.plans[n] = _lib.Plan(n, -1, "auto")
-        self.launches_per_step = sum(2 * self.plans[int(n)].launches(1) for n in ns)
+            k = int(np.sum(ns == n))
+            self.groups.append((_lib.Plan(n, -1, "auto"), pos, k))
+            pos += n * k
+        self.launches_per_step = sum(2 * p.launches(k) for p, _, k in self.groups) + 3
 
-    def forward(self, x, X, stream):
-        xp, Xp = x.data_ptr(), X.data_ptr()
-        for n, o in zip(self.ns, self.offs):
-            self.plans[int(n)].exec_ptr(xp + 8 * int(o), None, Xp + 8 * int(o), None, 1, stream)
-
-    def vjp(self, g, grad, stream):
-        gp, dp = g.data_ptr(), grad.data_ptr()
-        for n, o in zip(self.ns, self.offs):
-            self.plans[int(n)].exec_ptr(gp + 8 * int(o), None, dp + 8 * int(o), None, 1, stream, vjp=True)
+    def step(self, xg, wg, Xg, gradg, loss, stream):
+        import torch
+        xp, Xp, dp = xg.data_ptr(), Xg.data_ptr(), gradg.data_ptr()
+        for plan, start, k in self.groups:
+            plan.exec_ptr(xp + 8 * start, None, Xp + 8 * start, None, k, stream)
+        loss.copy_(torch.sum(wg * (Xg.real * Xg.real + Xg.imag * Xg.imag)).double().reshape(1))
+        Xg.mul_(2.0 * wg)
+        for plan, start, k in self.groups:
+            plan.exec_ptr(Xp + 8 * start, None, dp + 8 * start, None, k, stream, vjp=True)
 
 
 class BatchRunner:
@@ -390,18 +415,34 @@ def run_ours(args):
     lpins = [torch.zeros(1, dtype=torch.float64).pin_memory() for _ in range(2)]
     ms_e2e = time_e2e(sets, xpin, wpin, gpins, lpins, args.steps, 2, torch, dist)
 
-    # plain path (one plan exec per transform) for the "vs plain" ratio
-    ms_plain = None
+    # plain path (one launch per distinct length, graph-captured) for the
+    # "vs plain" ratio, timed like the batched step
+    ms_plain = plain_launches = None
     if not args.skip_plain and world == 1:
         plain = PlainRunner(ns)
-        xs_ = torch.cuda.current_stream().cuda_stream
+        gidx = torch.from_numpy(plain.gather).cuda()
+        xg, wg = x[gidx].contiguous(), w[gidx].contiguous()
+        Xg, gg = torch.empty_like(xg), torch.empty_like(xg)
+        lossg = torch.zeros(1, dtype=torch.float64, device="cuda")
 
         def plain_step():
-            plain.forward(x, cot, xs_)
-            g = cot * (2.0 * w)
-            plain.vjp(g, grad, xs_)
+            plain.step(xg, wg, Xg, gg, lossg, torch.cuda.current_stream().cuda_stream)
 
-        ms_plain = time_steps(plain_step, 2, 1, torch)
+        for _ in range(2):
+            plain_step()
+        torch.cuda.synchronize()
+        pgraph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(pgraph):
+            plain_step()
+        torch.cuda.synchronize()
+        ms_plain = time_steps(pgraph.replay, args.steps, args.warmup, torch)
+        plain_launches = plain.launches_per_step
+        # the plain path computes the same gradient
+        pgraph.replay()
+        step()
+        torch.cuda.synchronize()
+        plain_err = float((gg - grad[gidx]).norm() / grad[gidx].norm())
+        del pgraph, xg, wg, Xg, gg
 
     if rank != 0:
         dist.barrier()
@@ -428,11 +469,10 @@ def run_ours(args):
     # the dominant kernel is the tile kernel (every launch of the step); its
     # algorithmic bytes per step: read x, read w, write g, read g, write grad
     alg_bytes = total * (8 + 4 + 8 + 8 + 8)
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
-    # DRAM bytes of one step's tile-kernel launches (dram__bytes_read.sum +
-    # dram__bytes_write.sum from an ncu launch list of this workload with L2
-    # kept between launches); measured, not derived
-    traffic = STEP_DRAM_BYTES if args.count == COUNT else None
+    achieved = alg_bytes / ((ms_fwd + ms_vjp) * 1e-3) / 1e9
+    # DRAM bytes of one step's persistent launches, from the committed ncu
+    # summary (with the commit it was taken at, so that a stale figure shows)
+    traffic, traffic_commit = profiled_traffic() if args.count == COUNT else (None, None)
     cpu = None
     if not args.no_cpu and world == 1:
         v, cores, sample = cpu_baseline(ns)
@@ -443,21 +483,27 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
         "config": {"workload": "4096 mixed-size C2C transforms, n log-uniform [16, 65536] "
                                "(50% 5-smooth, 25% prime, 25% raw), fwd + cotangent + VJP",
-                   "sum_n": total, "path": "batched executor, CUDA graph",
+                   "sum_n": total, "path": "af_batch_* (one persistent launch per direction), CUDA graph",
                    "parallelism": f"replicas x{world} (no exchange)",
                    "l2": "inputs (267 MB) larger than L2",
                    "bytes_credited_per_step": "32 * sum(n) (16 N per transform application)",
                    "ms_forward_cotangent": ms_fwd, "ms_vjp": ms_vjp,
-                   "plain_ms_per_step": ms_plain, "speedup_vs_plain": (ms_plain / ms) if ms_plain else None},
+                   "plain_ms_per_step": ms_plain, "speedup_vs_plain": (ms_plain / ms) if ms_plain else None,
+                   "plain": "one af_exec_c2c + one af_vjp_c2c per distinct length over its length-grouped "
+                            "block, cotangent and loss as elementwise kernels, CUDA graph, same steps",
+                   "plain_launches_per_step": plain_launches,
+                   "plain_grad_rel_diff": plain_err if ms_plain else None},
         "e2e": {"value": world * nbytes / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
                 "note": "pinned H2D of x and w, the step, D2H of grad and loss, every step; double-buffered "
                         "so that copies overlap the neighbouring steps' transforms",
                 "h2d_bytes_per_step": int(xh.nbytes + wh.nbytes), "d2h_bytes_per_step": int(xh.nbytes + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "note": "tile kernel over the whole step: algorithmic 36 B per point "
-                             "(x, w, g, g, grad) / step time; peak = measured copy bandwidth; "
-                             "traffic = DRAM bytes per step (ncu)"},
+                     "traffic_source": f"{TRAFFIC_PROFILE} (ncu at commit {traffic_commit})" if traffic else None,
+                     "note": "the persistent kernel (every launch of the step): algorithmic 36 B per point "
+                             "(x, w read, g written; g read, grad written) / its two launches' time "
+                             "(CUDA events); peak = measured copy bandwidth (MEASURED_PEAKS.json); "
+                             "traffic = DRAM bytes per step"},
         "cpu_baseline": cpu,
         "gpu_launches": runner.launches_per_step * args.steps * world,
         "clocks": clk,
@@ -469,6 +515,244 @@ def run_ours(args):
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------- configs 1, 2, 3, 5
+def _peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)).get("hbm_gbs", 6800.0) if os.path.exists(path) else 6800.0
+
+
+def _err(y, ref):
+    y = np.asarray(y, dtype=np.complex128)
+    ref = np.asarray(ref, dtype=np.complex128)
+    return float(np.linalg.norm(y - ref) / np.linalg.norm(ref)), float(np.max(np.abs(y - ref)))
+
+
+def _cpu_c2c(ns, budget_s=8.0):
+    """The oracle (CPU restatement of the reference algorithm) in FP32 on the
+    host cores: forward + inverse-sign transforms of these lengths, repeated
+    for about budget_s."""
+    from oracle import oracle as O
+    nth = O.lib().or_max_threads()
+    ns = np.asarray(ns, dtype=np.int64)
+    fwd, inv = O.Mixed(ns, -1), O.Mixed(ns, +1)
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal(fwd.total) + 1j * rng.standard_normal(fwd.total)).astype(np.complex64)
+    X, G = np.empty_like(x), np.empty_like(x)
+    reps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s or reps == 0:
+        fwd.exec_f32(x, X, 0, len(ns), nth)
+        inv.exec_f32(X, G, 0, len(ns), nth)
+        reps += 1
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": 32 * int(ns.sum()) / dt / 1e9, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{len(ns)} transforms (sum n = {int(ns.sum())}), fwd + inverse-sign, {reps} reps"}
+
+
+def _line(cfg, workload, value, ms, steps, warmup, extra, alg_bytes, cpu, e2e_ms=None, h2d=0, d2h=0,
+          launches=None, clk=None, dtype="c64 (fp32)"):
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic", "config": dict({"config": cfg, "workload": workload}, **extra),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": _peak(), "unit": "GB/s",
+                         "frac": achieved / _peak(), "traffic": None},
+            "e2e": {"value": alg_bytes / (e2e_ms * 1e-3) / 1e9 if e2e_ms else None, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk}
+
+
+def _e2e(torch, fn, host_in, dev_in, dev_out, host_out, steps):
+    """Per-step time of: pinned H2D of the inputs, the call, D2H of the output."""
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        for h, d in zip(host_in, dev_in):
+            d.copy_(h, non_blocking=True)
+        fn()
+        host_out.copy_(dev_out, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_config(args):
+    import torch
+    from accelerate_fourier import _lib, convolution, planned, real
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    st = lambda: torch.cuda.current_stream().cuda_stream
+    steps, warm = args.steps, args.warmup
+    clocks = ClockSampler(0)
+    cfg = args.config
+    if cfg == 1:
+        n, B = 1024, 64
+        rng = np.random.default_rng(1)
+        xh = (rng.uniform(-1, 1, (B, n)) + 1j * rng.uniform(-1, 1, (B, n))).astype(np.complex64)
+        x = torch.from_numpy(xh).cuda()
+        X, y = torch.empty_like(x), torch.empty_like(x)
+        pf, pi = _lib.Plan(n, -1, "auto"), _lib.Plan(n, +1, "auto")
+
+        def step():
+            pf.exec_ptr(x.data_ptr(), None, X.data_ptr(), None, B, st())
+            pi.exec_ptr(X.data_ptr(), None, y.data_ptr(), None, B, st())
+            _lib.check(_lib.load().af_scale_down(0, y.data_ptr(), None, n, B, st()))
+
+        clocks.start()
+        ms = time_steps(step, steps, warm, torch)
+        clk = clocks.stop()
+        step()
+        torch.cuda.synchronize()
+        ref = O.planned(xh.astype(np.complex128), -1)
+        ef, mf = _err(X.cpu().numpy(), ref)
+        er, mr = _err(y.cpu().numpy(), xh)
+        xp, yp = torch.from_numpy(xh).pin_memory(), torch.empty_like(torch.from_numpy(xh)).pin_memory()
+        e2e = _e2e(torch, step, [xp], [x], y, yp, steps)
+        out = _line(1, "C2C N=1024 x 64, forward then inverse x 1/N (af_exec_c2c, af_scale_down)",
+                    32 * n * B / (ms * 1e-3) / 1e9, ms, steps, warm,
+                    {"rel_l2_forward_vs_fp64": ef, "max_abs_forward": mf, "rel_l2_round_trip": er,
+                     "max_abs_round_trip": mr, "bound": 4 * 2 ** -24 * 10, "note": "512 KB: launch-bound"},
+                    32 * n * B, _cpu_c2c([n] * B, 5.0), e2e, xh.nbytes, xh.nbytes,
+                    (pf.launches(B) + pi.launches(B) + 1) * steps, clk)
+    elif cfg == 2:
+        sizes = [1 << 20, 3 ** 12, 1001 * 1024, 65537, 1000003]
+        rng = np.random.default_rng(2)
+        per, tot_ms, tot_b, launches = [], 0.0, 0, 0
+        clocks.start()
+        for n in sizes:
+            xh = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+            x = torch.from_numpy(xh).cuda()
+            X = torch.empty_like(x)
+            p = _lib.Plan(n, -1, "auto")
+            f = lambda: p.exec_ptr(x.data_ptr(), None, X.data_ptr(), None, 1, st())
+            ms = time_steps(f, steps, warm, torch)
+            f()
+            torch.cuda.synchronize()
+            e, m = _err(X.cpu().numpy(), O.planned(xh.astype(np.complex128)[None], -1)[0])
+            per.append({"n": n, "plan": p.describe()[:60], "ms": ms, "GBs": 16 * n / (ms * 1e-3) / 1e9,
+                        "rel_l2_vs_fp64": e, "max_abs": m, "bound_4eps_log2n": 4 * 2 ** -24 * np.log2(n)})
+            tot_ms += ms
+            tot_b += 16 * n
+            launches += p.launches(1) * steps
+        clk = clocks.stop()
+        out = _line(2, "single large C2C transforms, batch 1 each: 2^20, 3^12, 1001*1024, 65537, 1000003 "
+                       "(af_exec_c2c)", tot_b / (tot_ms * 1e-3) / 1e9, tot_ms, steps, warm, {"sizes": per},
+                    tot_b, _cpu_c2c(sizes, 8.0), launches=launches, clk=clk)
+    elif cfg == 3:
+        rng = np.random.default_rng(3)
+        res = {}
+        clocks.start()
+        # R2C 2^24 x 8 through the half-length complex plan (Real.toSpectrum)
+        N, B = 1 << 24, 8
+        xr = rng.standard_normal((B, N)).astype(np.float32)
+        xd = torch.from_numpy(xr).cuda()
+        half = planned.transform(-1, N // 2)
+        ms_r = time_steps(lambda: real.toSpectrum(half, xd), steps, warm, torch)
+        spec = real.toSpectrum(half, xd)
+        torch.cuda.synchronize()
+        e, m = _err(spec[0].cpu().numpy(), O.to_spectrum(xr[:1].astype(np.float64))[0])
+        res["r2c"] = {"n": N, "batch": B, "ms": ms_r, "GBs": 12 * N * B / (ms_r * 1e-3) / 1e9,
+                      "bytes_per_point": "4 read + 8 written (full spectrum, as the reference)",
+                      "rel_l2_vs_fp64_row0": e, "max_abs_row0": m}
+        del xd, spec
+        # cyclic convolution of two length-2^20 signals (Planned.convolveCyclic, complex)
+        n = 1 << 20
+        a = rng.standard_normal(n) + 0j
+        b = rng.standard_normal(n) + 0j
+        ad = torch.from_numpy(a.astype(np.complex64)[None]).cuda()
+        bd = torch.from_numpy(b.astype(np.complex64)[None]).cuda()
+        conv = planned.convolveCyclic(n)
+        ms_c = time_steps(lambda: conv(ad, bd), steps, warm, torch)
+        z = conv(ad, bd)
+        torch.cuda.synchronize()
+        e, m = _err(z[0].cpu().numpy(), O.convolve_cyclic(a[None], b[None])[0])
+        res["cyclic_convolution"] = {"n": n, "ms": ms_c, "GBs": 24 * n / (ms_c * 1e-3) / 1e9,
+                                     "bytes_per_point": "two c64 inputs read, one c64 output written",
+                                     "rel_l2_vs_fp64": e, "max_abs": m}
+        # Karatsuba, Int32 4096 -> Int64, bit-exact
+        L = 4096
+        xi = rng.integers(-1000, 1001, (1, L)).astype(np.int32)
+        yi = rng.integers(-1000, 1001, (1, L)).astype(np.int32)
+        xk, yk = torch.from_numpy(xi).cuda(), torch.from_numpy(yi).cuda()
+        ms_k = time_steps(lambda: convolution.karatsuba(xk, yk), steps, warm, torch)
+        zk = convolution.karatsuba(xk, yk).cpu().numpy()
+        exact = np.convolve(xi[0].astype(np.int64), yi[0].astype(np.int64))
+        res["karatsuba"] = {"L": L, "ms": ms_k, "leaf_mults_per_s": 3 ** 12 / (ms_k * 1e-3),
+                            "bit_exact_vs_int64": bool(np.array_equal(zk[0], exact)),
+                            "bit_exact_vs_oracle": bool(np.array_equal(zk, O.karatsuba(xi, yi)))}
+        clk = clocks.stop()
+        tot_ms = ms_r + ms_c
+        tot_b = 12 * N * B + 24 * n
+        t0 = time.perf_counter()
+        O.to_spectrum(xr[:1].astype(np.float64))
+        O.convolve_cyclic(a[None], b[None])
+        dt = time.perf_counter() - t0
+        cpu = {"value": (12 * N + 24 * n) / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "one 2^24 R2C signal (of 8) and the 2^20 cyclic convolution, FP64 oracle, once"}
+        out = _line(3, "R2C 2^24 x 8 (af_to_spectrum), cyclic convolution 2^20 (af_convolve_cyclic), "
+                       "Karatsuba Int32 4096 -> Int64 (af_karatsuba_i32_i64)",
+                    tot_b / (tot_ms * 1e-3) / 1e9, tot_ms, steps, warm, res, tot_b, cpu, clk=clk)
+    else:  # 5: loss sum w |FFT x|^2, forward + VJP
+        res = {}
+        clocks.start()
+        tot_ms, tot_b = 0.0, 0
+        for label, n, B in (("c2c 2^16", 1 << 16, 256), ("bluestein 99991", 99991, 32)):
+            rng = np.random.default_rng(5)
+            xh = (rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n))).astype(np.complex64)
+            wh = rng.uniform(0, 1, (B, n)).astype(np.float32)
+            x, w = torch.from_numpy(xh).cuda(), torch.from_numpy(wh).cuda()
+            cot, grad = torch.empty_like(x), torch.empty_like(x)
+            loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+            bt = _lib.Batch([n] * B, -1)
+
+            def step():
+                bt.forward_cotangent_ptr(x.data_ptr(), w.data_ptr(), cot.data_ptr(), loss.data_ptr(), st())
+                bt.vjp_ptr(cot.data_ptr(), grad.data_ptr(), st())
+
+            ms = time_steps(step, steps, warm, torch)
+            step()
+            bt.status(st())
+            g = grad.cpu().numpy()
+            errs = []
+            for i in range(0, B, max(1, B // 4)):
+                X = np.fft.fft(xh[i].astype(np.complex128))
+                gref = np.fft.ifft(2 * wh[i] * X) * n  # 2 F^H (w . F x)
+                errs.append(_err(g[i], gref)[0])
+            res[label] = {"n": n, "batch": B, "ms": ms, "GBs": 32 * n * B / (ms * 1e-3) / 1e9,
+                          "grad_rel_l2_vs_fp64": max(errs), "launches_per_step": 2 * bt.launches()}
+            tot_ms += ms
+            tot_b += 32 * n * B
+            del x, w, cot, grad
+        # real FFT 2^18 x 32: toSpectrum forward, g = 2 w S, the toSpectrum VJP
+        n, B = 1 << 18, 32
+        rng = np.random.default_rng(5)
+        xr = rng.standard_normal((B, n)).astype(np.float32)
+        wr = rng.uniform(0, 1, (B, n)).astype(np.float32)
+        xd, wd = torch.from_numpy(xr).cuda(), torch.from_numpy(wr).cuda()
+        half = planned.transform(-1, n // 2)
+
+        def rstep():
+            S = real.toSpectrum(half, xd)
+            return real.toSpectrum_vjp(half, S * (2 * wd))
+
+        ms = time_steps(rstep, steps, warm, torch)
+        gr = rstep().cpu().numpy()
+        X = np.fft.fft(xr[0].astype(np.float64))
+        gref = np.real(np.fft.ifft(2 * wr[0] * X) * n)
+        res["real 2^18"] = {"n": n, "batch": B, "ms": ms, "GBs": 24 * n * B / (ms * 1e-3) / 1e9,
+                            "bytes_per_point": "4 read + 8 spectrum (forward), 8 + 4 (VJP)",
+                            "grad_rel_l2_vs_fp64_row0": _err(gr[0], gref)[0]}
+        tot_ms += ms
+        tot_b += 24 * n * B
+        clk = clocks.stop()
+        res["fd_check"] = "FP64 central finite differences: tests/test_gpu_grad.py"
+        out = _line(5, "loss sum w |FFT x|^2, forward + VJP: 256 x 2^16 and 32 x 99991 (af_batch_*), "
+                       "32 x real 2^18 (af_to_spectrum + af_vjp_to_spectrum)",
+                    tot_b / (tot_ms * 1e-3) / 1e9, tot_ms, steps, warm, res, tot_b,
+                    _cpu_c2c([1 << 16] * 8, 6.0), clk=clk)
+    print(json.dumps(out))
 
 
 def run_reference(args):
@@ -508,9 +792,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true", help="skip the plain-path comparison (profiling runs)")
     ap.add_argument("--count", type=int, default=COUNT, help="transforms in the workload (profiling runs use fewer)")
+    ap.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5],
+                    help="4: the batched mixed-size headline (default); 1, 2, 3, 5: the other configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != 4:
+        run_config(args)
     else:
         run_ours(args)
 
