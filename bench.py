@@ -105,6 +105,15 @@ def workload_sizes(count: int = COUNT, seed: int = 4):
     return np.array(out, dtype=np.int64)
 
 
+def parse_lengths(spec: str):
+    """Lengths given on the command line, e.g. "4096*2048,30011*64" (length*count)."""
+    out = []
+    for part in spec.split(","):
+        n, _, k = part.partition("*")
+        out += [int(n)] * int(k or 1)
+    return np.array(out, dtype=np.int64)
+
+
 # ----------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
@@ -354,7 +363,7 @@ def dist_setup(torch):
 def run_ours(args):
     import torch
     rank, world, dist = dist_setup(torch)
-    ns = workload_sizes(args.count)
+    ns = parse_lengths(args.lengths) if args.lengths else workload_sizes(args.count)
     total = int(ns.sum())
     nbytes = 32 * total
     rng = np.random.default_rng(5)
@@ -472,7 +481,7 @@ def run_ours(args):
     achieved = alg_bytes / ((ms_fwd + ms_vjp) * 1e-3) / 1e9
     # DRAM bytes of one step's persistent launches, from the committed ncu
     # summary (with the commit it was taken at, so that a stale figure shows)
-    traffic, traffic_commit = profiled_traffic() if args.count == COUNT else (None, None)
+    traffic, traffic_commit = profiled_traffic() if args.count == COUNT and not args.lengths else (None, None)
     cpu = None
     if not args.no_cpu and world == 1:
         v, cores, sample = cpu_baseline(ns)
@@ -792,6 +801,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true", help="skip the plain-path comparison (profiling runs)")
     ap.add_argument("--count", type=int, default=COUNT, help="transforms in the workload (profiling runs use fewer)")
+    ap.add_argument("--lengths", default="", help='profiling cases: "n*count,..." in place of the workload')
     ap.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5],
                     help="4: the batched mixed-size headline (default); 1, 2, 3, 5: the other configurations")
     args = ap.parse_args()
