@@ -85,14 +85,60 @@ void gen_root_tables(const std::vector<RootSeg>& segs, cx* dbase, cx* hbase, cud
 }
 
 // ============================================================ execution policies
+#ifdef __CUDACC__
+// the CTA's mbarrier of its bulk copies (namespace scope: shared memory)
+__shared__ unsigned long long s_mbar;
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+#endif
+// polls of a bulk copy's mbarrier before the CTA reports FE_TIMEOUT
+#define AFF_BULK_POLLS (1ll << 24)
+
 // Device: each phase is one call per thread followed by a barrier.
 struct DevExec {
   double loc = 0.0;  // the thread's running sum over every item it ran
+  unsigned par = 0;  // parity of the mbarrier phase the next bulk copy completes
+  unsigned* err = nullptr;  // the launch's error word
+  bool failed = false;      // a bulk copy of this CTA timed out (uniform after the phase's barrier)
 #ifdef __CUDACC__
   template <class F>
   __device__ __forceinline__ void phase(F&& f) {
     f((int)threadIdx.x);
     __syncthreads();
+  }
+  // A load phase whose main transfer is one bulk copy of `bytes` (a multiple
+  // of 16, both addresses 16-byte aligned) from global to shared memory,
+  // issued by thread 0 on the CTA's mbarrier; f issues the phase's other
+  // (cp.async) copies.  Each thread polls the mbarrier a bounded number of
+  // times; a copy that does not complete sets FE_TIMEOUT and marks the CTA
+  // failed.  After the wait the source lines `drop` .. `drop + drop_elems`
+  // (whole 128-byte lines, read by no other item) are discarded from L2, so
+  // that they are never written back.
+  template <class F>
+  __device__ __forceinline__ void phase_load(F&& f, cx* dst, const cx* src, unsigned bytes, const cx* drop,
+                                             i64 drop_elems) {
+    const unsigned mb = smem_u32(&s_mbar);
+    if (threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                       smem_u32(dst)),
+                   "l"(src), "r"(bytes), "r"(mb)
+                   : "memory");
+    }
+    f((int)threadIdx.x);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    unsigned done = 0;
+    for (long long k = 0; k < AFF_BULK_POLLS && !done; ++k)
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                   : "=r"(done)
+                   : "r"(mb), "r"(par)
+                   : "memory");
+    par ^= 1u;
+    if (!done) atomicExch(err + FC_ERROR, (unsigned)FE_TIMEOUT);
+    for (i64 i = 16 * (i64)threadIdx.x; i < drop_elems; i += 16 * (i64)blockDim.x)
+      asm volatile("discard.global.L2 [%0], 128;\n" ::"l"(drop + i) : "memory");
+    failed = __syncthreads_or(!done) != 0;
   }
   template <class F>
   __device__ __forceinline__ void phase_async(F&& f) {
@@ -128,6 +174,7 @@ struct DevExec {
 // Host: each phase runs for every thread index in turn.
 struct HostExec {
   int T;
+  bool failed = false;  // (host copies always complete)
   std::vector<double> locs;
   explicit HostExec(int t) : T(t), locs(t, 0.0) {}
   template <class F>
@@ -136,6 +183,11 @@ struct HostExec {
   }
   template <class F>
   void phase_async(F&& f) {
+    phase(f);
+  }
+  template <class F>
+  void phase_load(F&& f, cx* dst, const cx* src, unsigned bytes, const cx*, i64) {
+    memcpy(dst, src, bytes);
     phase(f);
   }
   template <class F>
@@ -415,6 +467,17 @@ AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, 
   }
 }
 
+// Lines cn..GL-1 of a loaded tile (the last block of a workspace region
+// holds lines past the transform, which no item writes) set to zero.
+#pragma nv_exec_check_disable
+template <int T, class E>
+AF_HD void zero_lines(E& ex, cx* a, int L, int GL, int cn) {
+  ex.phase([&](int tid) {
+    for (int i = tid; i < L * GL; i += T)
+      if ((i & (GL - 1)) >= cn) a[i] = make_cx(0.f, 0.f);
+  });
+}
+
 // sink of the direct items: bin m of transform q to the output
 struct DirectOut {
   Sink sk;
@@ -551,13 +614,14 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
     });
   }
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
+  const int lgb = ilog2i(x.gb);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int c = (int)fdiv((unsigned)u, S.L1div);
       const int k1 = u - c * L;
       const int j2 = c0 + c;
       const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-      A.ws[x.ws + (i64)j2 * L + k1] = v;
+      A.ws[x.ws + (i64)(k1 >> lgb) * x.s1 + j2 * x.gb + (k1 & (x.gb - 1))] = v;  // block k1 / gb
     }
   });
 }
@@ -571,10 +635,11 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int n1 = x.n1, c0 = it.c0, cn = it.cn;
-  ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, n1, L, cn, kAll);
-    copy_tables(tid, T, S, m);
-  });
+  // block c0 / GL of region 1, laid out as this item's tile
+  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
+  ex.phase_load([&](int tid) { copy_tables(tid, T, S, m); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk, x.s1);
+  if (ex.failed) return;
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
@@ -597,10 +662,11 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
   const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
   const int M1 = x.n1, c0 = it.c0, cn = it.cn;
-  ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogR, A.ws + x.ws + c0, M1, L, cn, kAll);
-    copy_multi_tables(tid, T, S, m, x);
-  });
+  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
+  ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
+                x.s1);
+  if (ex.failed) return;
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
   cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   ex.phase([&](int tid) {
@@ -625,12 +691,13 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
     }
   });
   res = run_line<T, SIGN>(ex, S, sm, nxt, res, m.tw);
+  const int lga = ilog2i(x.ga);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int l = (int)fdiv((unsigned)u, S.L1div);
       const int j2 = u - l * L;
       const int k1 = c0 + l;
-      A.ws[x.ws + x.M + (i64)k1 * L + j2] =
+      A.ws[x.ws2 + (i64)(j2 >> lga) * x.s2 + k1 * x.ga + (j2 & (x.ga - 1))] =  // block j2 / ga
           cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
     }
   });
@@ -645,10 +712,12 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
   const FXform& x = xf[0];
   const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
   const int M2 = x.n2, c0 = it.c0, cn = it.cn;
-  ex.phase_async([&](int tid) {
-    load_lines<true>(tid, T, m.a, GL, glogC, A.ws + x.ws + x.M + c0, M2, L, cn, kAll);
-    copy_multi_tables(tid, T, S, m, x);
-  });
+  // block c0 / GL of region 2, laid out as this item's tile
+  const cx* blk = A.ws + x.ws2 + (i64)(c0 >> glogC) * x.s2;
+  ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
+                x.s2);
+  if (ex.failed) return;
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
@@ -704,9 +773,15 @@ template <int T, int SIGN>
 __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitems, unsigned* ctrs,
                                                               long long spin_limit) {
   DevExec ex;
+  ex.err = ctrs;
   int loaded = -1;  // shape staged in s_shape (uniform across the CTA)
   int next = 0;     // thread 0: the item claimed for the next round
-  if (threadIdx.x == 0) next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+  if (threadIdx.x == 0) {
+    next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
   for (;;) {
     if (threadIdx.x == 0) {
       const int i = next;
@@ -739,6 +814,9 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
     __syncthreads();
     loaded = it.shape;
     run_item<T, SIGN>(ex, A, it, s_shape, s_xf, reinterpret_cast<cx*>(fsm4));
+    // a bulk copy that never completed: this CTA takes no further items (the
+    // items that wait for this one time out in turn)
+    if (ex.failed) break;
     if (it.done_ctr >= 0) {
       // every thread's stores of this item precede the barrier; thread 0's
       // fence then publishes them before the count

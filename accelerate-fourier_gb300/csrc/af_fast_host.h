@@ -60,7 +60,9 @@ enum { FE_OK = 0, FE_TIMEOUT = 1 };
 // One transform of the batch.
 struct FXform {
   i64 off;         // offset in the batch (complex units)
-  i64 ws;          // workspace offset (multi-pass schemes)
+  i64 ws, ws2;     // workspace regions 1 and 2 (multi-pass schemes; region 2: Bluestein)
+  int gb, s1;      // region 1: lines per block (the stage-B items' GL), block stride
+  int ga, s2;      // region 2: lines per block (the stage-A' items' GL), block stride
   int n;           // transform length
   int n1, n2;      // four-step split: n = n1 n2 (direct) or M = n1 n2 (Bluestein)
   int M;           // Bluestein convolution length

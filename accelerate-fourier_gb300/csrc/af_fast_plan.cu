@@ -193,9 +193,9 @@ struct FastBatch {
 
 // Every CTA of the persistent launch has 256 threads and the same shared
 // memory: three fit one SM (228 KB, less 1 KB reserved and the kernel's
-// 1.7 KB of staged descriptors per CTA).
+// 2.1 KB of staged descriptors and mbarrier per CTA).
 static const int kThreads = 256;
-static const int kCtaSmem = 74752;
+static const int kCtaSmem = 74496;
 static const int kMaxSmem = kCtaSmem;
 
 static size_t shape_smem(const FShape& s) {
@@ -504,13 +504,27 @@ static void plan_batch(FastBatch* B) {
     const int t = sp.t;
     const i64 n = B->ns[t];
     const i64 N = sp.N, n1 = sp.n1, n2 = sp.n2;  // length of the FFTs and its split
+    const int s1 = line_shape(B, (int)n1), s2 = line_shape(B, (int)n2);
+    const int C1 = B->shapes[s1].GL, C2 = B->shapes[s2].GL;
     FXform x = blank_xf(B->offs[t], n);
     x.n1 = (int)n1;
     x.n2 = (int)n2;
     x.M = (int)N;
+    // Workspace regions in blocks, one per consumer item, each laid out as
+    // that item's shared-memory tile and starting on a 128-byte line:
+    // region 1 (stage A -> stage B): block k1 / C2 holds (j2, k1) at
+    // j2 C2 + k1 mod C2; region 2 (Bluestein stage B -> A'): block j2 / C1
+    // holds (k1, j2) at k1 C1 + j2 mod C1.
+    auto up16 = [](i64 v) { return (v + 15) & ~(i64)15; };
+    x.gb = C2;
+    x.s1 = (int)up16(n2 * C2);
+    x.ga = C1;
+    x.s2 = blue ? (int)up16(n1 * C1) : 0;
+    const i64 r1 = (n1 + C2 - 1) / C2 * x.s1;
+    const i64 r2 = blue ? (n2 + C1 - 1) / C1 * x.s2 : 0;
     x.ws = B->ws_elems;
-    // Bluestein: pass R writes a second region; regions start on 128-byte lines
-    const i64 wsn = ((N + 15) & ~(i64)15) * (blue ? 2 : 1);
+    x.ws2 = x.ws + r1;
+    const i64 wsn = r1 + r2;
     B->ws_elems += wsn;
     i64 ct = -1, spec = -1;
     const i64 wt = table_tl3(B, N);
@@ -521,8 +535,6 @@ static void plan_batch(FastBatch* B) {
     }
     const int xi = (int)B->xf.size();
     push_xf(B, x, ct, wt, spec);
-    const int s1 = line_shape(B, (int)n1), s2 = line_shape(B, (int)n2);
-    const int C1 = B->shapes[s1].GL, C2 = B->shapes[s2].GL;
     MultiT mt;
     mt.ws = wsn;
     auto items = [&](int kind, int si, int C, i64 count) {
