@@ -133,7 +133,7 @@ static af_status exec_sign(af_plan plan, int sign, af_layout layout, const rl* i
   if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
   if (batch == 0 || plan->n == 0) return AF_OK;
   check_io(layout, in_re, in_im, out_re, out_im);
-  if (plan->n * batch >= ((i64)1 << 31)) return fail(AF_ERR_UNSUPPORTED, "n * batch must be below 2^31");
+  if (batch >= ((i64)1 << 31) / plan->n) return fail(AF_ERR_UNSUPPORTED, "n * batch must be below 2^31");
   Program& prog = program_for(plan, batch, sign);
   ensure_ws(plan, prog.ws_elems);
   const bool planar = layout == AF_LAYOUT_PLANAR;

@@ -11,10 +11,12 @@
 // holds these arrays (about 19 MiB) until the process exits.
 //
 // The first call on a device looks the arrays up with cudaGetSymbolAddress
-// (once per device, with that device current); make that first call before
-// any stream capture.  All calls share the arrays and each call overwrites
-// them, so calls that overlap on the GPU (on different streams) race; calls
-// in one stream are ordered.
+// (once per device, with that device current).  Every call uploads its launch
+// descriptors from host memory, so no call can be captured in a CUDA graph: a
+// call on a capturing stream fails with AF_ERR_UNSUPPORTED before it does
+// anything.  All calls share the arrays and each call overwrites them, so
+// calls that overlap on the GPU (on different streams) race; calls in one
+// stream are ordered.
 #include <mutex>
 
 #include "af_host.h"
@@ -80,11 +82,21 @@ extern "C" af_status af_exec_c2c_noalloc(int64_t n, int sign, const float* in, f
     if (n < 1 || (n & (n - 1))) return fail(AF_ERR_INVALID, "length must be a power of two");
     if (sign != 1 && sign != -1) return fail(AF_ERR_INVALID, "sign must be -1 (forward) or +1 (inverse)");
     if (batch < 0) return fail(AF_ERR_INVALID, "negative batch");
-    if (n * batch > kNoAllocMaxElems)
-      return fail(AF_ERR_INVALID, "n * batch = " + std::to_string(n * batch) + " exceeds the static workspace of " +
-                                      std::to_string(kNoAllocMaxElems) + " complex values");
+    // checked without forming n * batch, which could overflow
+    if (n > kNoAllocMaxElems || batch > kNoAllocMaxElems / n)
+      return fail(AF_ERR_INVALID, "n * batch (n = " + std::to_string(n) + ", batch = " + std::to_string(batch) +
+                                      ") exceeds the static workspace of " + std::to_string(kNoAllocMaxElems) +
+                                      " complex values");
     if (!in || !out) return fail(AF_ERR_INVALID, "null data pointer");
     if (((uintptr_t)in | (uintptr_t)out) & 7) return fail(AF_ERR_INVALID, "data must be 8-byte aligned");
+    // each call uploads its launch descriptors from host memory, which a
+    // stream capture cannot record: refuse before touching the stream
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+    if (ce != cudaSuccess) return fail(AF_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(ce));
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail(AF_ERR_UNSUPPORTED, "af_exec_c2c_noalloc cannot be captured in a CUDA graph: each call uploads its "
+                                      "launch descriptors from host memory");
     if (batch == 0) return AF_OK;
     NoAllocDevice dev;
     device_arrays(&dev);

@@ -711,16 +711,23 @@ size_t tile_smem_bytes(int smem_data, int tw_total, int G) {
 }
 
 // Raises the kernel's dynamic shared-memory limit to what the device allows
-// once per process (the opt-in limit less the kernel's static usage).
+// (the opt-in limit less the kernel's static usage), once per device: the
+// attribute is set per device, so a process using several GPUs sets it on
+// each the first time it launches there.
 template <int T, bool GEN>
 static cudaError_t launch_t(const LaunchSpec& L, const TileBases& bases, double* loss, cudaStream_t st) {
-  // set once per process; threads that race here compute and store the same value
-  static std::atomic<int> limit{-1};
-  if (limit.load(std::memory_order_acquire) < 0) {
-    int dev = 0, optin = 0;
+  // per device ordinal (0: not set yet; static storage starts at zero);
+  // threads that race here compute and store the same value
+  static std::atomic<int> limits[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::atomic<int>& limit = limits[dev];
+  if (limit.load(std::memory_order_acquire) <= 0) {
+    int optin = 0;
     cudaFuncAttributes fa;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, tile_kernel<T, GEN>);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(tile_kernel<T, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -327,9 +327,11 @@ af_status af_conv_complex_f64(int cyclic, const double* x_re, const double* x_im
  * Limit: n * batch <= 2^21 complex values; larger requests fail with
  * AF_ERR_INVALID and a message naming the limit.  The first call on a device
  * looks up the arrays' device addresses (once per device, with that device
- * current): make it before any stream capture.  All calls share the arrays
- * and each call overwrites them, so calls that overlap on the GPU race;
- * calls issued to one stream are ordered. */
+ * current).  Calls cannot be captured in a CUDA graph: every call uploads its
+ * launch descriptors from host memory, so a call on a capturing stream fails
+ * with AF_ERR_UNSUPPORTED and leaves the capture untouched.  All calls share
+ * the arrays and each call overwrites them, so calls that overlap on the GPU
+ * race; calls issued to one stream are ordered. */
 af_status af_exec_c2c_noalloc(int64_t n, int sign, const float* in, float* out,
                               int64_t batch, af_stream stream);
 
