@@ -9,28 +9,28 @@ from .sign import forward, inverse  # noqa: F401
 
 
 def ditSplitRadix(sign: int, length: int) -> Transform:
-    """Preprocessed.ditSplitRadix (Preprocessed.hs:433-444); length a power of two."""
+    """Preprocessed.ditSplitRadix (Preprocessed.hs:53-93); length a power of two."""
     return Transform(sign, length, "prep_splitradix")
 
 
 def dit2(sign: int, length: int) -> Transform:
-    """Preprocessed.dit2 (Preprocessed.hs:479-491); length a power of two."""
+    """Preprocessed.dit2 (Preprocessed.hs:99-111); length a power of two."""
     return Transform(sign, length, "prep_dit2")
 
 
 def dif2(sign: int, length: int) -> Transform:
-    """Preprocessed.dif2 (Preprocessed.hs:497-515); length a power of two."""
+    """Preprocessed.dif2 (Preprocessed.hs:117-135); length a power of two."""
     return Transform(sign, length, "prep_dif2")
 
 
 def transform2d(transform0: Transform, transform1: Transform):
-    """Preprocessed.transform2d (Preprocessed.hs:136-149): transform0 along the
+    """Preprocessed.transform2d (Preprocessed.hs:142-148): transform0 along the
     last axis, transform1 along the second-to-last."""
     from .planned import TransformND
     return TransformND(transform0, transform1)
 
 
 def transform3d(transform0: Transform, transform1: Transform, transform2: Transform):
-    """Preprocessed.transform3d (Preprocessed.hs:151-160)."""
+    """Preprocessed.transform3d (Preprocessed.hs:154-160)."""
     from .planned import TransformND
     return TransformND(transform0, transform1, transform2)

@@ -53,9 +53,9 @@ typedef enum {
   AF_ALGO_DECOMPOSE = 1,       /* Planned.transformDecompose (Planned.hs:114-119) */
   AF_ALGO_CHIRP2 = 2,          /* Planned.transformChirp2    (Planned.hs:704-708) */
   AF_ALGO_CHIRP235 = 3,        /* Planned.transformChirp235  (Planned.hs:716-720) */
-  AF_ALGO_PREP_DIT2 = 4,       /* Preprocessed.dit2          (Preprocessed.hs:479-491) */
-  AF_ALGO_PREP_DIF2 = 5,       /* Preprocessed.dif2          (Preprocessed.hs:497-515) */
-  AF_ALGO_PREP_SPLITRADIX = 6, /* Preprocessed.ditSplitRadix (Preprocessed.hs:433-444) */
+  AF_ALGO_PREP_DIT2 = 4,       /* Preprocessed.dit2          (Preprocessed.hs:99-111) */
+  AF_ALGO_PREP_DIF2 = 5,       /* Preprocessed.dif2          (Preprocessed.hs:117-135) */
+  AF_ALGO_PREP_SPLITRADIX = 6, /* Preprocessed.ditSplitRadix (Preprocessed.hs:53-93) */
   AF_ALGO_ADHOC_AUTO = 7,      /* Adhoc.transform            (Adhoc.hs:74-84)   */
   AF_ALGO_ADHOC_DIT2 = 8,      /* Adhoc.dit2                 (Adhoc.hs:138-153) */
   AF_ALGO_ADHOC_SPLITRADIX = 9,/* Adhoc.ditSplitRadix        (Adhoc.hs:101-108) */

@@ -8,7 +8,8 @@ own source documents in comments, read from the reference source tree.
     5, the permutation `Permutation.T` and the permuted matrix (transform5).
 
 The fixture is committed; the tests read it and never the reference tree.
-Run from the repository root:  python tests/golden/make_reference_tables.py [REFERENCE_ROOT]
+Run from the repository root:  python tests/golden/make_reference_tables.py REFERENCE_ROOT
+(REFERENCE_ROOT: the root of the accelerate-fourier source tree)
 """
 import json
 import os
@@ -87,4 +88,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_reference_tables.py REFERENCE_ROOT  (the accelerate-fourier source tree)")
+    main(sys.argv[1])
