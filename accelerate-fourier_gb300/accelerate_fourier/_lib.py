@@ -68,6 +68,8 @@ SIGNATURES = {
     "af_batch_vjp": ([PTR, PTR, PTR, PTR], INT),
     "af_batch_forward_cotangent": ([PTR, PTR, PTR, PTR, PTR, PTR], INT),
     "af_batch_status": ([PTR, PTR], INT),
+    "af_batch_create_tuned": ([ctypes.POINTER(PTR), PTR, I64, INT, ctypes.c_char_p, PTR], INT),
+    "af_batch_describe": ([PTR, ctypes.c_char_p, ctypes.c_size_t], INT),
     "af_exec_c2c_noalloc": ([I64, INT, PTR, PTR, I64, PTR], INT),
     "af_cyclic_reverse_2d": ([INT, PTR, PTR, PTR, PTR, I64, I64, I64, PTR], INT),
     "af_exec_c2c_axis": ([PTR, INT, PTR, PTR, PTR, PTR, I64, I64, PTR], INT),
@@ -192,14 +194,27 @@ class Plan:
 class Batch:
     """An af_batch: many transforms of mixed lengths stored back to back."""
 
-    def __init__(self, lengths, sign: int = -1):
+    def __init__(self, lengths, sign: int = -1, tune_cache=None, tune: bool = False, stream=0):
+        """tune (or a tune_cache path): the planner choices are timed on the
+        device (af_batch_create_tuned) and kept in tune_cache when given."""
         import numpy as np
         self.lengths = np.ascontiguousarray(np.asarray(lengths, dtype=np.int64))
         self.sign = int(sign)
         self.total = int(self.lengths.sum())
         self._h = PTR()
-        check(load().af_batch_create(ctypes.byref(self._h), self.lengths.ctypes.data, len(self.lengths),
-                                     self.sign))
+        if tune or tune_cache:
+            path = str(tune_cache).encode() if tune_cache else None
+            check(load().af_batch_create_tuned(ctypes.byref(self._h), self.lengths.ctypes.data, len(self.lengths),
+                                               self.sign, path, stream))
+        else:
+            check(load().af_batch_create(ctypes.byref(self._h), self.lengths.ctypes.data, len(self.lengths),
+                                         self.sign))
+
+    def describe(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(load().af_batch_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def launches(self) -> int:
         out = I64()

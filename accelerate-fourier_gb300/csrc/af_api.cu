@@ -18,6 +18,9 @@ cudaError_t fast_exec(FastBatch* B, int sign, const float2* in, float2* out, con
                       cudaStream_t st);
 int fast_status(FastBatch* B, cudaStream_t st);
 bool fast_supports(const i64* ns, i64 count);
+FastBatch* fast_create_tuned(const i64* ns, i64 count, const char* cache_path, cudaStream_t st, std::string* report);
+std::string fast_tuning(FastBatch* B);
+std::string fast_describe(FastBatch* B);
 bool fast_poison_wait(FastBatch* B, long long spin_limit);
 }  // namespace af
 
@@ -27,6 +30,7 @@ struct af_batch_s {
   af::FastBatch* f = nullptr;
   af::BatchPlan* b = nullptr;
   int sign = -1;
+  std::string autotune;  // the autotuner's report (af_batch_create_tuned)
   ~af_batch_s() {
     af::fast_destroy(f);
     af::batch_destroy(b);
@@ -141,6 +145,46 @@ af_status af_batch_create(af_batch* batch, const int64_t* lengths, int64_t count
     throw;
   }
   *batch = B;
+  return AF_OK;
+  AF_CATCH
+}
+
+af_status af_batch_create_tuned(af_batch* batch, const int64_t* lengths, int64_t count, int sign,
+                                const char* cache_path, af_stream stream) {
+  AF_TRY
+  if (!batch || (!lengths && count)) return fail(AF_ERR_INVALID, "null argument");
+  *batch = nullptr;
+  if (count < 0) return fail(AF_ERR_INVALID, "negative count");
+  if (sign != 1 && sign != -1) return fail(AF_ERR_INVALID, "sign must be -1 or +1");
+  af_batch_s* B = new af_batch_s();
+  B->sign = sign;
+  try {
+    if (fast_supports((const i64*)lengths, count))
+      B->f = fast_create_tuned((const i64*)lengths, count, cache_path, (cudaStream_t)stream, &B->autotune);
+    else
+      B->b = batch_create((const i64*)lengths, count, sign);
+  } catch (...) {
+    delete B;
+    throw;
+  }
+  *batch = B;
+  return AF_OK;
+  AF_CATCH
+}
+
+af_status af_batch_describe(af_batch batch, char* buf, size_t len) {
+  AF_TRY
+  if (!batch || !buf) return fail(AF_ERR_INVALID, "null argument");
+  std::string s;
+  if (batch->f)
+    s = "{\"executor\": \"persistent\", \"plan\": " + fast_describe(batch->f) + ", \"tuning\": " +
+        fast_tuning(batch->f) + (batch->autotune.empty() ? std::string() : ", \"autotune\": " +
+                                 (batch->autotune == "cached" ? std::string("\"cached\"") : batch->autotune)) +
+        "}";
+  else
+    s = "{\"executor\": \"multi-launch\", \"launches\": " + std::to_string(batch_launches(batch->b)) + "}";
+  if (s.size() + 1 > len) return fail(AF_ERR_INVALID, "buffer too small");
+  memcpy(buf, s.c_str(), s.size() + 1);
   return AF_OK;
   AF_CATCH
 }

@@ -2,6 +2,8 @@
 // root tables and launches for a list of transform lengths, and the internal
 // afx_fast_* entry points the tests use (device runs and host emulation).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -818,6 +820,200 @@ bool fast_poison_wait(FastBatch* B, long long spin_limit) {
     return true;
   }
   return false;
+}
+
+int fast_status(FastBatch* B, cudaStream_t st);
+
+// ------------------------------------------------------------ autotuner
+// The planner's choices are timed on the device for the batch at hand: from
+// the defaults, each choice in turn (stage slack, lines per multi-pass item,
+// radix-16 passes with the compile-time lines, item size) takes the value
+// with the shortest forward launch, the others held.  Operation counts do
+// not predict the time (the reference's planner says as much of its own
+// algorithm choice, Planned.hs:206-214); the launch is timed with CUDA events,
+// three warm-up launches then five timed ones, on zero data.  The winner is
+// kept as one JSON line per (GPU name, batch) in `cache_path` (when given):
+//   {"gpu": "...", "key": "<count>:<hash of the lengths>", "tune": [...], "ms": t, "default_ms": t0}
+static std::string tune_key(const i64* ns, i64 count) {
+  unsigned long long h = 1469598103934665603ull;  // FNV-1a over the lengths
+  for (i64 i = 0; i < count; ++i) {
+    unsigned long long v = (unsigned long long)ns[i];
+    for (int b = 0; b < 8; ++b) {
+      h ^= (v >> (8 * b)) & 0xffu;
+      h *= 1099511628211ull;
+    }
+  }
+  std::ostringstream o;
+  o << count << ":" << std::hex << h;
+  return o.str();
+}
+
+static std::string gpu_name() {
+  int dev = 0;
+  cudaDeviceProp p;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown";
+  std::string n(p.name);
+  for (char& c : n)
+    if (c == '"' || c == '\\') c = ' ';
+  return n;
+}
+
+static const int kTuneFields = 7;
+static void tune_to(const FastTune& t, int* v) {
+  v[0] = t.radix16;
+  v[1] = t.gl_max;
+  v[2] = t.balance_v;
+  v[3] = t.target;
+  v[4] = t.slack;
+  v[5] = t.l2_mb;
+  v[6] = t.fixed;
+}
+
+// the cached choice for (gpu, key), if any
+static bool tune_lookup(const char* path, const std::string& gpu, const std::string& key, int* v, double* ms) {
+  if (!path) return false;
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  const std::string g = "\"gpu\": \"" + gpu + "\"", k = "\"key\": \"" + key + "\"";
+  while (fgets(line, sizeof line, f)) {
+    const std::string ln(line);
+    if (ln.find(g) == std::string::npos || ln.find(k) == std::string::npos) continue;
+    const size_t p = ln.find("\"tune\": [");
+    const size_t q = ln.find("\"ms\": ");
+    if (p == std::string::npos || q == std::string::npos) continue;
+    int t[kTuneFields];
+    if (sscanf(ln.c_str() + p, "\"tune\": [%d, %d, %d, %d, %d, %d, %d]", &t[0], &t[1], &t[2], &t[3], &t[4], &t[5],
+               &t[6]) != kTuneFields)
+      continue;
+    memcpy(v, t, sizeof t);
+    *ms = atof(ln.c_str() + q + 6);
+    found = true;  // the last matching line wins
+  }
+  fclose(f);
+  return found;
+}
+
+static void tune_store(const char* path, const std::string& gpu, const std::string& key, const int* v, double ms,
+                       double ms0) {
+  if (!path) return;
+  FILE* f = fopen(path, "a");
+  if (!f) return;
+  fprintf(f, "{\"gpu\": \"%s\", \"key\": \"%s\", \"tune\": [%d, %d, %d, %d, %d, %d, %d], \"ms\": %.4f, \"default_ms\": %.4f}\n",
+          gpu.c_str(), key.c_str(), v[0], v[1], v[2], v[3], v[4], v[5], v[6], ms, ms0);
+  fclose(f);
+}
+
+// mean time of one forward launch of B over zero data
+static double time_batch(FastBatch* B, cx* in, cx* out, cudaStream_t st) {
+  cudaEvent_t e0, e1;
+  fcheck(cudaEventCreate(&e0), "tuning events");
+  fcheck(cudaEventCreate(&e1), "tuning events");
+  float ms = 0.f;
+  try {
+    for (int i = 0; i < 3; ++i) fcheck(fast_exec(B, -1, in, out, nullptr, nullptr, st), "tuning launch");
+    fcheck(cudaEventRecord(e0, st), "tuning events");
+    for (int i = 0; i < 5; ++i) fcheck(fast_exec(B, -1, in, out, nullptr, nullptr, st), "tuning launch");
+    fcheck(cudaEventRecord(e1, st), "tuning events");
+    fcheck(cudaEventSynchronize(e1), "tuning events");
+    fcheck(cudaEventElapsedTime(&ms, e0, e1), "tuning events");
+    if (fast_status(B, st) != FE_OK) throw FastError("a tuning launch timed out");
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / 5.0;
+}
+
+FastBatch* fast_create_tuned(const i64* ns, i64 count, const char* cache_path, cudaStream_t st, std::string* report) {
+  const std::string key = tune_key(ns, count), gpu = gpu_name();
+  int best[kTuneFields];
+  double best_ms = 0;
+  if (tune_lookup(cache_path, gpu, key, best, &best_ms)) {
+    if (report) *report = "cached";
+    return fast_create(ns, count, false, best, kTuneFields);
+  }
+  i64 total = 0;
+  for (i64 i = 0; i < count; ++i) total += ns[i];
+  cx *in = nullptr, *out = nullptr;
+  fcheck(cudaMalloc(&in, sizeof(cx) * std::max<i64>(total, 1)), "tuning buffers");
+  if (cudaMalloc(&out, sizeof(cx) * std::max<i64>(total, 1)) != cudaSuccess) {
+    cudaFree(in);
+    throw FastError("tuning buffers: out of device memory");
+  }
+  std::ostringstream rep;
+  double ms0 = 0;
+  try {
+    fcheck(cudaMemsetAsync(in, 0, sizeof(cx) * std::max<i64>(total, 1), st), "tuning buffers");
+    auto measure = [&](const int* v) {
+      FastBatch* B = fast_create(ns, count, false, v, kTuneFields);
+      double t;
+      try {
+        t = time_batch(B, in, out, st);
+      } catch (...) {
+        fast_destroy(B);
+        throw;
+      }
+      fast_destroy(B);
+      rep << (rep.tellp() > 0 ? ", " : "") << "[" << v[0] << "," << v[1] << "," << v[2] << "," << v[3] << "," << v[4]
+          << "," << v[5] << "," << v[6] << "]: " << t;
+      return t;
+    };
+    FastTune d;
+    tune_to(d, best);
+    best_ms = ms0 = measure(best);
+    // coordinate descent over the choices, each value tried with the others held
+    const struct {
+      int field;
+      std::vector<int> values;
+    } axes[] = {{4, {912, 2736}}, {1, {16, 64}}, {0, {0}}, {3, {3072}}};
+    for (const auto& ax : axes)
+      for (int val : ax.values) {
+        int cand[kTuneFields];
+        memcpy(cand, best, sizeof cand);
+        if (cand[ax.field] == val) continue;
+        cand[ax.field] = val;
+        double t;
+        try {
+          t = measure(cand);
+        } catch (const FastError&) {
+          continue;  // a choice the planner refuses for this batch
+        }
+        if (t < best_ms) {
+          best_ms = t;
+          memcpy(best, cand, sizeof best);
+        }
+      }
+  } catch (...) {
+    cudaFree(in);
+    cudaFree(out);
+    throw;
+  }
+  cudaFree(in);
+  cudaFree(out);
+  tune_store(cache_path, gpu, key, best, best_ms, ms0);
+  if (report) {
+    std::ostringstream o;
+    o << "{\"tune\": [" << best[0] << ", " << best[1] << ", " << best[2] << ", " << best[3] << ", " << best[4] << ", "
+      << best[5] << ", " << best[6] << "], \"ms\": " << best_ms << ", \"default_ms\": " << ms0
+      << ", \"candidates\": \"" << rep.str() << "\"}";
+    *report = o.str();
+  }
+  return fast_create(ns, count, false, best, kTuneFields);
+}
+
+// the planner choices the batch was made with, as a JSON list (FastTune order)
+std::string fast_tuning(FastBatch* B) {
+  int v[kTuneFields];
+  tune_to(B->tune, v);
+  std::ostringstream o;
+  o << "[" << v[0] << ", " << v[1] << ", " << v[2] << ", " << v[3] << ", " << v[4] << ", " << v[5] << ", " << v[6]
+    << "]";
+  return o.str();
 }
 
 // FE_OK or FE_TIMEOUT of the last launch (waits for it to finish)

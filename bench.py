@@ -254,10 +254,17 @@ class BatchRunner:
     every signal with the fused epilogue g = 2 w X, loss = sum w |X|^2) and
     af_batch_vjp (grad = DFT^H g)."""
 
-    def __init__(self, ns):
+    def __init__(self, ns, tune=True):
+        import tempfile
         from accelerate_fourier import _lib
-        self.batch = _lib.Batch(ns, -1)
-        self.launches_per_step = 2 * self.batch.launches()  # tile kernels (the loss reset is a memset)
+        t0 = time.perf_counter()
+        # planner choices timed on this GPU (af_batch_create_tuned); the cache
+        # lives in a fresh temporary file, so every run tunes
+        cache = os.path.join(tempfile.mkdtemp(prefix="af_tune_"), "tune.jsonl") if tune else None
+        self.batch = _lib.Batch(ns, -1, tune=tune, tune_cache=cache)
+        self.create_s = time.perf_counter() - t0
+        self.describe = self.batch.describe()
+        self.launches_per_step = 2 * self.batch.launches()  # persistent launches (the loss reset is a memset)
 
     def step(self, x, w, cot, grad, loss, stream):
         self.batch.forward_cotangent_ptr(x.data_ptr(), w.data_ptr(), cot.data_ptr(), loss.data_ptr(), stream)
@@ -498,6 +505,8 @@ def run_ours(args):
                    "bytes_credited_per_step": "32 * sum(n) (16 N per transform application)",
                    "ms_forward_cotangent": ms_fwd, "ms_vjp": ms_vjp,
                    "plain_ms_per_step": ms_plain, "speedup_vs_plain": (ms_plain / ms) if ms_plain else None,
+                   "autotune": runner.describe.get("autotune"), "tuning": runner.describe.get("tuning"),
+                   "batch_create_s": runner.create_s,
                    "plain": "one af_exec_c2c + one af_vjp_c2c per distinct length over its length-grouped "
                             "block, cotangent and loss as elementwise kernels, CUDA graph, same steps",
                    "plain_launches_per_step": plain_launches,

@@ -156,6 +156,18 @@ af_status af_cyclic_reverse_2d(af_layout layout, const float* in_re,
  * this entry point is the batched form of that call. */
 typedef struct af_batch_s* af_batch;
 af_status af_batch_create(af_batch* batch, const int64_t* lengths, int64_t count, int sign);
+/* af_batch_create with the persistent executor's planner choices (stage
+ * slack, lines per multi-pass item, radix-16 passes, item size) picked by
+ * timing candidate plans of these lengths on the current device, on
+ * `stream`; the choice is appended to the JSON-lines file `cache_path` (NULL:
+ * no cache) under the GPU's name and a hash of the lengths, and reused from
+ * there by later calls.  No counterpart in the reference, whose planner
+ * (Planned.hs:206-214) picks algorithms by operation counts only. */
+af_status af_batch_create_tuned(af_batch* batch, const int64_t* lengths, int64_t count, int sign,
+                                const char* cache_path, af_stream stream);
+/* JSON description of the batch: the executor, its work items, the planner
+ * choices and the autotuner's report.  No counterpart in the reference. */
+af_status af_batch_describe(af_batch batch, char* buf, size_t len);
 af_status af_batch_destroy(af_batch batch);
 af_status af_batch_launches(af_batch batch, int64_t* launches);
 /* out = transform of every in (sign of the batch). */

@@ -174,3 +174,25 @@ def test_stage_wait_timeout_is_reported_and_the_device_stays_usable():
     ys = run(make_batch(sizes, -1), xs)
     for n, xi, yi in zip(sizes, split(xs, sizes), split(ys, sizes)):
         assert rel_l2(yi, O().planned(xi[None], -1)[0]) <= fp32_bound(n, 4.0), int(n)
+
+
+def test_tuned_batch_matches_oracle_and_reuses_its_cache(tmp_path):
+    """af_batch_create_tuned times candidate planner choices on the device,
+    keeps the winner in the cache file, and a second creation reuses it."""
+    from accelerate_fourier import _lib
+    sizes = np.array([64, 1000, 4099, 20000, 30011, 16000, 65536], dtype=np.int64)
+    cache = tmp_path / "tune.jsonl"
+    b = _lib.Batch(sizes, -1, tune_cache=cache)
+    d = b.describe()
+    assert d["executor"] == "persistent"
+    assert d["autotune"]["ms"] <= d["autotune"]["default_ms"]
+    assert d["tuning"] == d["autotune"]["tune"]
+    assert cache.exists() and len(cache.read_text().splitlines()) == 1
+    b2 = _lib.Batch(sizes, -1, tune_cache=cache)
+    assert b2.describe()["autotune"] == "cached"
+    assert b2.describe()["tuning"] == d["tuning"]
+    rng = np.random.default_rng(18)
+    x = crand(rng, int(sizes.sum()), "normal")
+    y = run(b2, x)
+    for n, xi, yi in zip(sizes, split(x, sizes), split(y, sizes)):
+        assert rel_l2(yi, O().planned(xi[None], -1)[0]) <= fp32_bound(n, 4.0), int(n)
