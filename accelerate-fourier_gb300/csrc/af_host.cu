@@ -5,7 +5,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <complex>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -13,58 +12,36 @@
 
 namespace AF_NS {
 
-typedef std::complex<double> cd;
-
-// ============================================================ host FP64 FFT
-// Used once per plan for the Rader kernel spectrum and the Bluestein chirp
-// spectrum, whose inputs are generated on the device in FP64.
-static int smallest_factor(i64 n) {
-  for (i64 p = 2; p * p <= n && p <= 64; ++p)
-    if (n % p == 0) return (int)p;
-  return n <= 64 ? (int)n : 0;
-}
-
-static void fft64(const cd* x, i64 xs, cd* y, i64 n, int sign);
-
-static void bluestein64(const cd* x, i64 xs, cd* y, i64 n, int sign) {
-  const i64 M = ceiling_power_of_two(2 * n - 1);
-  std::vector<cd> ch(n), a(M, 0.0), b(M, 0.0), A(M), B(M), C(M);
-  for (i64 k = 0; k < n; ++k) {
-    const unsigned long long r = (unsigned long long)((__int128)k * k % (2 * n));
-    const double ang = M_PI * (double)r / (double)n;
-    ch[k] = cd(std::cos(ang), sign * std::sin(ang));
-  }
-  for (i64 k = 0; k < n; ++k) a[k] = ch[k] * x[k * xs];
-  for (i64 k = 0; k < n; ++k) {
-    b[k] = std::conj(ch[k]);
-    if (k) b[M - k] = std::conj(ch[k]);
-  }
-  fft64(a.data(), 1, A.data(), M, -1);
-  fft64(b.data(), 1, B.data(), M, -1);
-  for (i64 i = 0; i < M; ++i) A[i] *= B[i];
-  fft64(A.data(), 1, C.data(), M, 1);
-  for (i64 k = 0; k < n; ++k) y[k] = ch[k] * C[k] / (double)M;
-}
-
-static void fft64(const cd* x, i64 xs, cd* y, i64 n, int sign) {
-  if (n == 1) { y[0] = x[0]; return; }
-  const int r = smallest_factor(n);
-  if (r == 0) { bluestein64(x, xs, y, n, sign); return; }
-  const i64 m = n / r;
-  std::vector<cd> sub(n);
-  for (int s = 0; s < r; ++s) fft64(x + s * xs, xs * r, sub.data() + s * m, m, sign);
-  std::vector<cd> w(n);
-  for (i64 t = 0; t < n; ++t) {
-    const double ang = 2.0 * M_PI * (double)t / (double)n;
-    w[t] = cd(std::cos(ang), sign * std::sin(ang));
-  }
-  for (i64 k = 0; k < m; ++k)
-    for (int q = 0; q < r; ++q) {
-      cd acc = 0;
-      const i64 kk = k + q * m;
-      for (int s = 0; s < r; ++s) acc += sub[s * m + k] * w[(i64)((__int128)s * kk % n)];
-      y[kk] = acc;
+// ============================================================ FP64 spectra on the device
+// The Rader kernel spectrum and the Bluestein chirp spectrum of a plan are
+// FP64 transforms of tables generated on the device in FP64; they run on the
+// device with the library's own Complex Double engine (an FP64 plan of the
+// spectrum's length; its own Rader and Bluestein spectra come the same way,
+// over shorter lengths), then are scaled and rounded to the element type.
+struct DevBufs {
+  std::vector<void*> p;
+  double2* get(i64 n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, sizeof(double2) * (size_t)std::max<i64>(n, 1)) != cudaSuccess) {
+      cudaGetLastError();
+      throw AfError(AF_ERR_ALLOC, "cudaMalloc of a spectrum buffer failed");
     }
+    p.push_back(q);
+    return (double2*)q;
+  }
+  ~DevBufs() {
+    for (void* q : p) cudaFree(q);
+  }
+};
+
+// y = DFT of x (n points, sign as given, unscaled) in FP64 on the device
+static void dev_fft64(const double2* x, double2* y, i64 n, int sign) {
+  af_plan p = nullptr;
+  if (af_plan_create_f64(&p, n, sign, AF_ALGO_AUTO) != AF_OK)
+    throw AfError(AF_ERR_CUDA, std::string("FP64 spectrum plan: ") + af_last_error());
+  const af_status st = af_exec_c2c_f64(p, AF_LAYOUT_INTERLEAVED, (const double*)x, nullptr, (double*)y, nullptr, 1, 0);
+  af_plan_destroy(p);
+  if (st != AF_OK) throw AfError(AF_ERR_CUDA, std::string("FP64 spectrum transform: ") + af_last_error());
 }
 
 // ============================================================ resources
@@ -151,12 +128,6 @@ const cx* PlanRes::pair_table(i64 a, i64 b, int* off_b) {
   return p;
 }
 
-static std::vector<cx> to_cx(const std::vector<cd>& v) {
-  std::vector<cx> o(v.size());
-  for (size_t i = 0; i < v.size(); ++i) o[i] = make_cx((rl)v[i].real(), (rl)v[i].imag());
-  return o;
-}
-
 // Length of the transforms carrying a Rader convolution of length p-1:
 // p-1 itself when it is 13-smooth (the reference's Rader), otherwise the
 // least 13-smooth M >= 2(p-1)-1, so that the cyclic convolution of length p-1
@@ -214,27 +185,23 @@ const RaderRes& PlanRes::rader_res(i64 p, int sign) {
   cuda_check(cudaMemcpy(r.src, src.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.inv, inv.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
   cuda_check(cudaMemcpy(r.gpow, gpow.data(), sizeof(int) * m, cudaMemcpyHostToDevice), "rader tables");
-  // kernel in FP64 on the device, spectrum in FP64 on the host
-  double2* dk = nullptr;
-  cuda_check(cudaMalloc(&dk, sizeof(double2) * m), "rader kernel");
-  cudaError_t e = launch_rader_kernel(dk, p, r.g, sign, 0);
-  std::vector<cd> kern(m);
-  if (e == cudaSuccess) e = cudaMemcpy(kern.data(), dk, sizeof(double2) * m, cudaMemcpyDeviceToHost);
-  cudaFree(dk);
-  cuda_check(e, "rader kernel");
-  // cyclic convolution of length m computed with transforms of length M >= m:
-  // the kernel is placed periodically, kk[i] = k[i], kk[M-i] = k[m-i] (0 < i < m);
-  // for M = m this is the reference's kernel spectrum
-  std::vector<cd> kk(M, cd(0, 0)), S(M);
-  for (i64 i = 0; i < m; ++i) kk[i] = kern[i];
-  if (M > m)
-    for (i64 i = 1; i < m; ++i) kk[M - i] = kern[m - i];
-  fft64(kk.data(), 1, S.data(), M, +1);
-  for (auto& v : S) v /= (double)M;
-  std::vector<cx> zs = to_cx(S);
-  r.zs = (cx*)dalloc(sizeof(cx) * M);
-  r.M = M;
-  cuda_check(cudaMemcpy(r.zs, zs.data(), sizeof(cx) * M, cudaMemcpyHostToDevice), "rader spectrum");
+  // kernel and spectrum in FP64 on the device.  The cyclic convolution of
+  // length m is computed with transforms of length M >= m: the kernel is
+  // placed periodically, kk[i] = k[i], kk[M-i] = k[m-i] (0 < i < m); for
+  // M = m this is the reference's kernel spectrum
+  {
+    DevBufs tmp;
+    double2* dk = tmp.get(m);
+    double2* kk = tmp.get(M);
+    double2* S = tmp.get(M);
+    cuda_check(launch_rader_kernel(dk, p, r.g, sign, 0), "rader kernel");
+    cuda_check(launch_spectrum_input(dk, m, kk, M, 0, 0), "rader kernel");
+    dev_fft64(kk, S, M, +1);
+    r.zs = (cx*)dalloc(sizeof(cx) * M);
+    r.M = M;
+    cuda_check(launch_scale_round(S, r.zs, M, 1.0 / (double)M, 0), "rader spectrum");
+    cuda_check(cudaStreamSynchronize(0), "rader spectrum");
+  }
   rader[key] = r;
   return rader[key];
 }
@@ -254,22 +221,21 @@ const ChirpRes& PlanRes::chirp_res(i64 len, i64 pad, int sign) {
     chirps[key] = c;
     return chirps[key];
   }
-  double2* dc = nullptr;
-  cuda_check(cudaMalloc(&dc, sizeof(double2) * pad), "chirp");
-  cudaError_t e = launch_chirp(dc, pad, len, sign, pad, 0);
-  std::vector<cd> ch(pad), cj(pad), spec(pad);
-  if (e == cudaSuccess) e = cudaMemcpy(ch.data(), dc, sizeof(double2) * pad, cudaMemcpyDeviceToHost);
-  cudaFree(dc);
-  cuda_check(e, "chirp");
-  for (i64 i = 0; i < pad; ++i) cj[i] = std::conj(ch[i]);
-  fft64(cj.data(), 1, spec.data(), pad, +1);
-  for (auto& v : spec) v /= (double)pad;
-  std::vector<cd> head(ch.begin(), ch.begin() + len);
-  std::vector<cx> hf = to_cx(head), sf = to_cx(spec);
-  c.chirp = (cx*)dalloc(sizeof(cx) * len);
-  c.spec = (cx*)dalloc(sizeof(cx) * pad);
-  cuda_check(cudaMemcpy(c.chirp, hf.data(), sizeof(cx) * len, cudaMemcpyHostToDevice), "chirp");
-  cuda_check(cudaMemcpy(c.spec, sf.data(), sizeof(cx) * pad, cudaMemcpyHostToDevice), "chirp");
+  // chirp and spectrum in FP64 on the device
+  {
+    DevBufs tmp;
+    double2* dc = tmp.get(pad);
+    double2* cj = tmp.get(pad);
+    double2* S = tmp.get(pad);
+    cuda_check(launch_chirp(dc, pad, len, sign, pad, 0), "chirp");
+    cuda_check(launch_spectrum_input(dc, pad, cj, pad, 1, 0), "chirp");
+    dev_fft64(cj, S, pad, +1);
+    c.chirp = (cx*)dalloc(sizeof(cx) * len);
+    c.spec = (cx*)dalloc(sizeof(cx) * pad);
+    cuda_check(launch_scale_round(dc, c.chirp, len, 1.0, 0), "chirp");
+    cuda_check(launch_scale_round(S, c.spec, pad, 1.0 / (double)pad, 0), "chirp");
+    cuda_check(cudaStreamSynchronize(0), "chirp");
+  }
   chirps[key] = c;
   return chirps[key];
 }

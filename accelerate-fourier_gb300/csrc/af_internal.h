@@ -63,6 +63,8 @@ cudaError_t launch_twiddle_table(cx* dst, i64 n, int S, int H, cudaStream_t st);
 cudaError_t launch_chirp(double2* dst, i64 pad, i64 len, int sign, i64 count, cudaStream_t st);
 // Rader kernel[i] = exp(sign * 2 pi i * (g^i mod p) / p) (Planned.hs:655-659)
 cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st);
+cudaError_t launch_spectrum_input(const double2* k, i64 m, double2* kk, i64 M, int conj, cudaStream_t st);
+cudaError_t launch_scale_round(const double2* S, cx* out, i64 n, double s, cudaStream_t st);
 
 // ------------------------------------------------------------- real / two-real / convolution maps
 // A complex array: interleaved when c is set, else planar re/im.

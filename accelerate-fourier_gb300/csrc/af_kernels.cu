@@ -2,6 +2,8 @@
 // (Good-Thomas CRT maps, Rader permutations, cyclic reverse), pointwise
 // spectrum products, and the FP64 generators of twiddle, chirp and Rader
 // kernel tables.
+#include <algorithm>
+
 #include "af_internal.h"
 
 namespace AF_NS {
@@ -138,6 +140,35 @@ __global__ void rader_kernel_kernel(double2* dst, i64 p, i64 g, int sign) {
 cudaError_t launch_rader_kernel(double2* dst, i64 p, i64 g, int sign, cudaStream_t st) {
   const i64 cnt = p - 1;
   rader_kernel_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(dst, p, g, sign);
+  return cudaGetLastError();
+}
+
+// The input of a spectrum table: k (m entries) placed periodically over M >= m
+// (kk[i] = k[i] for i < m, kk[M - j] = k[m - j] for 0 < j < m when M > m,
+// zero elsewhere), conjugated when conj != 0.
+__global__ void spectrum_input_kernel(const double2* k, i64 m, double2* kk, i64 M, int conj) {
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (i64)gridDim.x * blockDim.x) {
+    double2 v = make_double2(0.0, 0.0);
+    if (i < m) v = k[i];
+    else if (M > m && M - i < m) v = k[m - (M - i)];
+    if (conj) v.y = -v.y;
+    kk[i] = v;
+  }
+}
+cudaError_t launch_spectrum_input(const double2* k, i64 m, double2* kk, i64 M, int conj, cudaStream_t st) {
+  const i64 blocks = std::min<i64>((M + 255) / 256, 4096);
+  spectrum_input_kernel<<<(unsigned)blocks, 256, 0, st>>>(k, m, kk, M, conj);
+  return cudaGetLastError();
+}
+
+// out[i] = S[i] * s in the element type (FP64 values rounded for Complex Float)
+__global__ void scale_round_kernel(const double2* S, cx* out, i64 n, double s) {
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+    out[i] = make_cx((rl)(S[i].x * s), (rl)(S[i].y * s));
+}
+cudaError_t launch_scale_round(const double2* S, cx* out, i64 n, double s, cudaStream_t st) {
+  const i64 blocks = std::min<i64>((n + 255) / 256, 4096);
+  scale_round_kernel<<<(unsigned)blocks, 256, 0, st>>>(S, out, n, s);
   return cudaGetLastError();
 }
 
