@@ -400,34 +400,34 @@ template <> struct Dft<5> {
 // and rounded to the element type).
 template <int R> struct OddRoots;
 template <> struct OddRoots<7> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[4] = {1.0f, 0.62348980185873359439, -0.22252093395631433737, -0.90096886790241903498};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[4] = {0.0f, 0.78183148246802980363, 0.97492791218182361934, 0.43388373911755823142};
     return v[m];
   }
 };
 template <> struct OddRoots<11> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[6] = {1.0f, 0.84125353283118120551, 0.41541501300188643508, -0.14231483827328500480,
                             -0.65486073394528498959, -0.95949297361449736865};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[6] = {0.0f, 0.54064081745559755543, 0.90963199535451833011, 0.98982144188093279524,
                             0.75574957435425826890, 0.28173255684142967104};
     return v[m];
   }
 };
 template <> struct OddRoots<13> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[7] = {1.0f, 0.88545602565320991051, 0.56806474673115592289, 0.12053668025532300601,
                             -0.35460488704253545489, -0.74851074817110119231, -0.97094181742605201180};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[7] = {0.0f, 0.46472317204376850652, 0.82298386589365635224, 0.99270887409805397272,
                             0.93501624268541483342, 0.66312265824079519305, 0.23931566428755768339};
     return v[m];
@@ -478,91 +478,101 @@ template <> struct Dft<13> : DftOdd<13> {};
 // rounded to the element type).
 template <int R> struct Roots;
 template <> struct Roots<6> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[6] = {1.00000000000000000000e+00, 5.00000000000000111022e-01, -4.99999999999999777955e-01, -1.00000000000000000000e+00, -5.00000000000000444089e-01, 5.00000000000000111022e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[6] = {0.00000000000000000000e+00, 8.66025403784438596588e-01, 8.66025403784438707611e-01, 0.00000000000000000000e+00, -8.66025403784438374544e-01, -8.66025403784438596588e-01};
     return v[m];
   }
 };
 template <> struct Roots<9> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[9] = {1.00000000000000000000e+00, 7.66044443118978013452e-01, 1.73648177666930414453e-01, -4.99999999999999777955e-01, -9.39692620785908316883e-01, -9.39692620785908427905e-01, -5.00000000000000444089e-01, 1.73648177666929970364e-01, 7.66044443118977791407e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[9] = {0.00000000000000000000e+00, 6.42787609686539251896e-01, 9.84807753012208020316e-01, 8.66025403784438707611e-01, 3.42020143325668879442e-01, -3.42020143325668657397e-01, -8.66025403784438374544e-01, -9.84807753012208131338e-01, -6.42787609686539584963e-01};
     return v[m];
   }
 };
 template <> struct Roots<10> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[10] = {1.00000000000000000000e+00, 8.09016994374947451263e-01, 3.09016994374947451263e-01, -3.09016994374947340241e-01, -8.09016994374947340241e-01, -1.00000000000000000000e+00, -8.09016994374947562285e-01, -3.09016994374947562285e-01, 3.09016994374947229218e-01, 8.09016994374947340241e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[10] = {0.00000000000000000000e+00, 5.87785252292473137103e-01, 9.51056516295153531182e-01, 9.51056516295153642204e-01, 5.87785252292473248126e-01, 0.00000000000000000000e+00, -5.87785252292473026081e-01, -9.51056516295153531182e-01, -9.51056516295153642204e-01, -5.87785252292473359148e-01};
     return v[m];
   }
 };
 template <> struct Roots<12> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[12] = {1.00000000000000000000e+00, 8.66025403784438707611e-01, 5.00000000000000111022e-01, 0.00000000000000000000e+00, -4.99999999999999777955e-01, -8.66025403784438707611e-01, -1.00000000000000000000e+00, -8.66025403784438818633e-01, -5.00000000000000444089e-01, 0.00000000000000000000e+00, 5.00000000000000111022e-01, 8.66025403784438374544e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[12] = {0.00000000000000000000e+00, 4.99999999999999944489e-01, 8.66025403784438596588e-01, 1.00000000000000000000e+00, 8.66025403784438707611e-01, 4.99999999999999944489e-01, 0.00000000000000000000e+00, -4.99999999999999722444e-01, -8.66025403784438374544e-01, -1.00000000000000000000e+00, -8.66025403784438596588e-01, -5.00000000000000444089e-01};
     return v[m];
   }
 };
 template <> struct Roots<15> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[15] = {1.00000000000000000000e+00, 9.13545457642600866599e-01, 6.69130606358858237570e-01, 3.09016994374947451263e-01, -1.04528463267653332069e-01, -4.99999999999999777955e-01, -8.09016994374947340241e-01, -9.78147600733805688833e-01, -9.78147600733805688833e-01, -8.09016994374947562285e-01, -5.00000000000000444089e-01, -1.04528463267654234126e-01, 3.09016994374947229218e-01, 6.69130606358858459615e-01, 9.13545457642600977621e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[15] = {0.00000000000000000000e+00, 4.06736643075800152758e-01, 7.43144825477394133095e-01, 9.51056516295153531182e-01, 9.94521895368273400884e-01, 8.66025403784438707611e-01, 5.87785252292473248126e-01, 2.07911690817759314820e-01, -2.07911690817759065020e-01, -5.87785252292473026081e-01, -8.66025403784438374544e-01, -9.94521895368273289861e-01, -9.51056516295153642204e-01, -7.43144825477394022073e-01, -4.06736643075800152758e-01};
     return v[m];
   }
 };
 template <> struct Roots<20> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[20] = {1.00000000000000000000e+00, 9.51056516295153531182e-01, 8.09016994374947451263e-01, 5.87785252292473137103e-01, 3.09016994374947451263e-01, 0.00000000000000000000e+00, -3.09016994374947340241e-01, -5.87785252292473026081e-01, -8.09016994374947340241e-01, -9.51056516295153531182e-01, -1.00000000000000000000e+00, -9.51056516295153753227e-01, -8.09016994374947562285e-01, -5.87785252292473248126e-01, -3.09016994374947562285e-01, 0.00000000000000000000e+00, 3.09016994374947229218e-01, 5.87785252292472915059e-01, 8.09016994374947340241e-01, 9.51056516295153531182e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[20] = {0.00000000000000000000e+00, 3.09016994374947395752e-01, 5.87785252292473137103e-01, 8.09016994374947451263e-01, 9.51056516295153531182e-01, 1.00000000000000000000e+00, 9.51056516295153642204e-01, 8.09016994374947451263e-01, 5.87785252292473248126e-01, 3.09016994374947506774e-01, 0.00000000000000000000e+00, -3.09016994374946896151e-01, -5.87785252292473026081e-01, -8.09016994374947340241e-01, -9.51056516295153531182e-01, -1.00000000000000000000e+00, -9.51056516295153642204e-01, -8.09016994374947562285e-01, -5.87785252292473359148e-01, -3.09016994374947617796e-01};
     return v[m];
   }
 };
+template <> struct Roots<24> {
+  static AF_HD rl c(int m) {
+    constexpr rl v[24] = {1.00000000000000000000e+00, 9.65925826289068312214e-01, 8.66025403784438707611e-01, 7.07106781186547572737e-01, 5.00000000000000111022e-01, 2.58819045102520739476e-01, 6.12323399573676603587e-17, -2.58819045102520628454e-01, -4.99999999999999777955e-01, -7.07106781186547461715e-01, -8.66025403784438707611e-01, -9.65925826289068201191e-01, -1.00000000000000000000e+00, -9.65925826289068312214e-01, -8.66025403784438818633e-01, -7.07106781186547905804e-01, -5.00000000000000444089e-01, -2.58819045102520628454e-01, -1.83697019872102968750e-16, 2.58819045102520295387e-01, 5.00000000000000111022e-01, 7.07106781186547350693e-01, 8.66025403784438374544e-01, 9.65925826289068090169e-01};
+    return v[m];
+  }
+  static AF_HD rl s(int m) {
+    constexpr rl v[24] = {0.00000000000000000000e+00, 2.58819045102520739476e-01, 4.99999999999999944489e-01, 7.07106781186547461715e-01, 8.66025403784438596588e-01, 9.65925826289068312214e-01, 1.00000000000000000000e+00, 9.65925826289068312214e-01, 8.66025403784438707611e-01, 7.07106781186547572737e-01, 4.99999999999999944489e-01, 2.58819045102521017032e-01, 1.22464679914735320717e-16, -2.58819045102520794988e-01, -4.99999999999999722444e-01, -7.07106781186547128648e-01, -8.66025403784438374544e-01, -9.65925826289068312214e-01, -1.00000000000000000000e+00, -9.65925826289068423236e-01, -8.66025403784438596588e-01, -7.07106781186547683760e-01, -5.00000000000000444089e-01, -2.58819045102521572144e-01};
+    return v[m];
+  }
+};
 template <> struct Roots<25> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[25] = {1.00000000000000000000e+00, 9.68583161128631076053e-01, 8.76306680043863583940e-01, 7.28968627421411552447e-01, 5.35826794978996545638e-01, 3.09016994374947451263e-01, 6.27905195293135265366e-02, -1.87381314585724600974e-01, -4.25779291565072715020e-01, -6.37423989748689745483e-01, -8.09016994374947340241e-01, -9.29776485888251347234e-01, -9.92114701314477764882e-01, -9.92114701314477875904e-01, -9.29776485888251458256e-01, -8.09016994374947784330e-01, -6.37423989748689523438e-01, -4.25779291565072159909e-01, -1.87381314585724628730e-01, 6.27905195293128326472e-02, 3.09016994374947229218e-01, 5.35826794978996767682e-01, 7.28968627421411219380e-01, 8.76306680043863139851e-01, 9.68583161128630965031e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[25] = {0.00000000000000000000e+00, 2.48689887164854794843e-01, 4.81753674101715323452e-01, 6.84547105928688615073e-01, 8.44327925502015075310e-01, 9.51056516295153531182e-01, 9.98026728428271558968e-01, 9.82287250728688721146e-01, 9.04827052466019465804e-01, 7.70513242775789253258e-01, 5.87785252292473248126e-01, 3.68124552684678141290e-01, 1.25333233564304535879e-01, -1.25333233564304286078e-01, -3.68124552684677919245e-01, -5.87785252292472693014e-01, -7.70513242775789364281e-01, -9.04827052466019798871e-01, -9.82287250728688721146e-01, -9.98026728428271558968e-01, -9.51056516295153642204e-01, -8.44327925502014964287e-01, -6.84547105928688948140e-01, -4.81753674101716100608e-01, -2.48689887164855349955e-01};
     return v[m];
   }
 };
 template <> struct Roots<27> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[27] = {1.00000000000000000000e+00, 9.73044870579823806267e-01, 8.93632640323412275052e-01, 7.66044443118978013452e-01, 5.97158591702786178956e-01, 3.96079766039156899726e-01, 1.73648177666930414453e-01, -5.81448289104757737311e-02, -2.86803232711090205775e-01, -4.99999999999999777955e-01, -6.86241637868733489469e-01, -8.35487811412936265398e-01, -9.39692620785908316883e-01, -9.93238357741943023171e-01, -9.93238357741943023171e-01, -9.39692620785908538927e-01, -8.35487811412936487443e-01, -6.86241637868733600492e-01, -5.00000000000000444089e-01, -2.86803232711090649865e-01, -5.81448289104762386370e-02, 1.73648177666930830787e-01, 3.96079766039156511148e-01, 5.97158591702785845889e-01, 7.66044443118977791407e-01, 8.93632640323412164030e-01, 9.73044870579824028312e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[27] = {0.00000000000000000000e+00, 2.30615870742440165486e-01, 4.48799180200462166646e-01, 6.42787609686539251896e-01, 8.02123192755043734614e-01, 9.18216106880273996715e-01, 9.84807753012208020316e-01, 9.98308158271268175632e-01, 9.57989512315488900285e-01, 8.66025403784438707611e-01, 7.27373641573048845821e-01, 5.49508978070806231031e-01, 3.42020143325668879442e-01, 1.16092914125229929034e-01, -1.16092914125230123323e-01, -3.42020143325668213308e-01, -5.49508978070806008986e-01, -7.27373641573048623776e-01, -8.66025403784438374544e-01, -9.57989512315488789262e-01, -9.98308158271268175632e-01, -9.84807753012208020316e-01, -9.18216106880274107738e-01, -8.02123192755043956659e-01, -6.42787609686539584963e-01, -4.48799180200462444201e-01, -2.30615870742439582619e-01};
     return v[m];
   }
 };
 template <> struct Roots<32> {
-  static __device__ __forceinline__ rl c(int m) {
+  static AF_HD rl c(int m) {
     constexpr rl v[32] = {1.00000000000000000000e+00, 9.80785280403230430579e-01, 9.23879532511286738483e-01, 8.31469612302545235671e-01, 7.07106781186547572737e-01, 5.55570233019602288671e-01, 3.82683432365089837290e-01, 1.95090322016128331351e-01, 0.00000000000000000000e+00, -1.95090322016128192573e-01, -3.82683432365089726268e-01, -5.55570233019601955604e-01, -7.07106781186547461715e-01, -8.31469612302545346694e-01, -9.23879532511286738483e-01, -9.80785280403230430579e-01, -1.00000000000000000000e+00, -9.80785280403230430579e-01, -9.23879532511286849505e-01, -8.31469612302545457716e-01, -7.07106781186547683760e-01, -5.55570233019602177649e-01, -3.82683432365090336891e-01, -1.95090322016128664417e-01, 0.00000000000000000000e+00, 1.95090322016128303595e-01, 3.82683432365090003824e-01, 5.55570233019601844582e-01, 7.07106781186547350693e-01, 8.31469612302545235671e-01, 9.23879532511286516439e-01, 9.80785280403230319557e-01};
     return v[m];
   }
-  static __device__ __forceinline__ rl s(int m) {
+  static AF_HD rl s(int m) {
     constexpr rl v[32] = {0.00000000000000000000e+00, 1.95090322016128248084e-01, 3.82683432365089781779e-01, 5.55570233019602177649e-01, 7.07106781186547461715e-01, 8.31469612302545235671e-01, 9.23879532511286738483e-01, 9.80785280403230430579e-01, 1.00000000000000000000e+00, 9.80785280403230430579e-01, 9.23879532511286738483e-01, 8.31469612302545457716e-01, 7.07106781186547572737e-01, 5.55570233019602177649e-01, 3.82683432365089892802e-01, 1.95090322016128608906e-01, 0.00000000000000000000e+00, -1.95090322016128359106e-01, -3.82683432365089670757e-01, -5.55570233019601955604e-01, -7.07106781186547461715e-01, -8.31469612302545235671e-01, -9.23879532511286516439e-01, -9.80785280403230319557e-01, -1.00000000000000000000e+00, -9.80785280403230430579e-01, -9.23879532511286627461e-01, -8.31469612302545457716e-01, -7.07106781186547683760e-01, -5.55570233019602177649e-01, -3.82683432365090392402e-01, -1.95090322016128719929e-01};
     return v[m];
   }
@@ -570,7 +580,7 @@ template <> struct Roots<32> {
 
 // multiply by exp(sign * 2 pi i m / R) for a compile-time m (after unrolling)
 template <int R>
-__device__ __forceinline__ cx mul_root(cx a, int m, rl sign) {
+AF_HD cx mul_root(cx a, int m, rl sign) {
   m %= R;
   if (m == 0) return a;
   if (4 * m == R) return mul_si(a, sign);
@@ -583,7 +593,7 @@ __device__ __forceinline__ cx mul_root(cx a, int m, rl sign) {
 // of u[B j1 + j2], twiddle W_R^(j2 k1), DFT_B over j2; output k1 + A k2.
 template <int A, int B>
 struct DftComposite {
-  static __device__ __forceinline__ void run(cx* u, rl sign, const cx* tab, int S, int n) {
+  static AF_HD void run(cx* u, rl sign, const cx* tab, int S, int n) {
     constexpr int R = A * B;
     cx v[R];
 #pragma unroll
@@ -612,6 +622,7 @@ template <> struct Dft<10> : DftComposite<2, 5> {};
 template <> struct Dft<12> : DftComposite<4, 3> {};
 template <> struct Dft<15> : DftComposite<3, 5> {};
 template <> struct Dft<20> : DftComposite<4, 5> {};
+template <> struct Dft<24> : DftComposite<8, 3> {};
 template <> struct Dft<25> : DftComposite<5, 5> {};
 template <> struct Dft<27> : DftComposite<3, 9> {};
 template <> struct Dft<32> : DftComposite<4, 8> {};

@@ -330,7 +330,7 @@ template <int T, int SIGN, class E>
 AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
   if (S.fixed) {  // a compile-time line (the planner sets `fixed` only for listed pairs)
     switch (S.line.L * 1024 + S.GL) {
-#define AFF_FIXED_CASE(L, GL)                              \
+#define AFF_FIXED_CASE(L, GL, R1, R2)                      \
   case L * 1024 + GL:                                      \
     cline_passes<T, SIGN, L, GL, 0>(ex, src, dst, tw);     \
     return src;

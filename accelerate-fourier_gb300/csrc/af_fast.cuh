@@ -174,24 +174,35 @@ AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, in
 }
 
 // ------------------------------------------------------------ compile-time lines
-// A line FFT whose length L and line count GL are template constants runs
-// the passes the planner makes for it (radix 16s, 8s, 5s, one 4, 3s, 2s;
-// two lines per unit except at radix 16; m-major twiddles at the same table
-// offsets), with every stride, loop bound and divisor known to the compiler.
-// AFF_FIXED_LINES lists the (L, GL) pairs compiled this way.
-// The lengths are those whose pairwise products serve as the Bluestein
-// convolution lengths of the multi-pass scheme; GL is the planner's line
-// count for each under the default tuning.
-#define AFF_FIXED_LINES(X)                                                                                     \
-  X(64, 32) X(80, 32) X(96, 32) X(100, 32) X(120, 32) X(128, 32) X(144, 16) X(160, 16) X(180, 16) X(192, 16) \
-  X(200, 16) X(216, 16) X(240, 16) X(250, 16) X(256, 16) X(270, 8) X(288, 8) X(300, 8) X(320, 8) X(360, 8)     \
-  X(384, 8) X(400, 8) X(432, 8) X(480, 8) X(500, 4) X(512, 4)
+// A line FFT whose length L and line count GL are template constants runs in
+// two passes of radices R1 then R2 (L = R1 R2; radices above 8 are done in
+// registers as composite butterflies, Cooley-Tukey inside the butterfly with
+// constant roots), one line per unit above radix 8 and two lines per unit at
+// 8 and below, the pass-2 twiddles W_L^(k m) m-major in shared memory, with
+// every stride, loop bound and divisor known to the compiler.
+// AFF_FIXED_LINES lists (L, GL, R1, R2): the lengths whose pairwise products
+// serve as the Bluestein convolution lengths of the multi-pass scheme, GL the
+// planner's line count for each under the default tuning.
+#define AFF_FIXED_LINES(X)                                                                                    \
+  X(64, 32, 16, 4) X(80, 32, 16, 5) X(96, 32, 16, 6) X(100, 32, 10, 10) X(120, 32, 15, 8) X(128, 32, 16, 8) \
+  X(144, 16, 16, 9) X(160, 16, 16, 10) X(180, 16, 15, 12) X(192, 16, 16, 12) X(200, 16, 20, 10)             \
+  X(216, 16, 24, 9) X(240, 16, 16, 15) X(250, 16, 25, 10) X(256, 16, 16, 16) X(270, 8, 27, 10)              \
+  X(288, 8, 32, 9) X(300, 8, 20, 15) X(320, 8, 16, 20) X(360, 8, 24, 15) X(384, 8, 32, 12) X(400, 8, 20, 20) \
+  X(432, 8, 27, 16) X(480, 8, 32, 15) X(500, 4, 25, 20) X(512, 4, 32, 16)
 
 struct CRadices {
   int n;
   int r[AFF_MAXPASS];
 };
-constexpr CRadices c_radices(int L) {
+// the radices of a line: the listed pair for a compile-time line, else 16s,
+// 8s, 5s, one 4, 3s, 2s
+constexpr CRadices c_radices(int L, bool fixed = true) {
+  if (fixed) {
+#define AFF_FIXED_SPLIT(l, g, r1, r2) \
+  if (L == l) return CRadices{2, {r1, r2}};
+    AFF_FIXED_LINES(AFF_FIXED_SPLIT)
+#undef AFF_FIXED_SPLIT
+  }
   CRadices x{0, {}};
   int m = L;
   while (m % 16 == 0) { x.r[x.n++] = 16; m /= 16; }
@@ -232,13 +243,13 @@ AF_HD void cpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, int b, i
   }
   const int q = b / P;
   const int k = b - q * P;
-  if (P > 1 && k > 0) {
-    cx w[R];
-    pass_twiddles<R>(tw, k, P, w);
+  if (P > 1 && k > 0) {  // each twiddle applied as it is read (few live registers)
 #pragma unroll
-    for (int m = 1; m < R; ++m)
+    for (int m = 1; m < R; ++m) {
+      const cx w = tw[(m - 1) * P + k];
 #pragma unroll
-      for (int v = 0; v < V; ++v) a[v][m] = cmul_s<SIGN>(a[v][m], w[m]);
+      for (int v = 0; v < V; ++v) a[v][m] = cmul_s<SIGN>(a[v][m], w);
+    }
   }
 #pragma unroll
   for (int v = 0; v < V; ++v) Dft<R>::run(a[v], (rl)SIGN, nullptr, 0, 0);
@@ -273,7 +284,7 @@ AF_HD void cline_passes(E& ex, cx*& src, cx*& dst, const cx* tw) {
   constexpr CRadices rs = c_radices(L);
   if constexpr (J < rs.n) {
     constexpr int R = rs.r[J], P = c_span(L, J), NB = L / R;
-    constexpr int V = (GL >= 2 && R != 16) ? 2 : 1;
+    constexpr int V = (GL >= 2 && R <= 8) ? 2 : 1;
     constexpr int LSo = J == rs.n - 1 ? (L | 1) : 0;
     constexpr int TW = c_twoff(L, J);
     cx* s = src;

@@ -43,7 +43,7 @@ struct FastTune {
 static const std::vector<int>& fixed_lengths() {
   static const std::vector<int> v = [] {
     std::vector<int> r;
-#define AFF_FIXED_LEN(l, g) r.push_back(l);
+#define AFF_FIXED_LEN(l, g, r1, r2) r.push_back(l);
     AFF_FIXED_LINES(AFF_FIXED_LEN)
 #undef AFF_FIXED_LEN
     return r;
@@ -88,16 +88,21 @@ static FixedProduct fixed_split(i64 n) {
 }
 
 static bool is_fixed_line(int L, int GL) {
-#define AFF_FIXED_TEST(l, g) if (L == l && GL == g) return true;
+#define AFF_FIXED_TEST(l, g, r1, r2) if (L == l && GL == g) return true;
   AFF_FIXED_LINES(AFF_FIXED_TEST)
 #undef AFF_FIXED_TEST
   return false;
 }
 
-// Radices of a 5-smooth line length: 16s or 8s first (the first pass has no
-// twiddles), then 5, 4, 3, 2.
-static std::vector<int> line_radices(int L, bool r16) {
+// Radices of a 5-smooth line length: the two listed radices of a compile-time
+// line (fixed), else 16s or 8s first (the first pass has no twiddles), then
+// 5, 4, 3, 2.
+static std::vector<int> line_radices(int L, bool r16, bool fixed = false) {
   std::vector<int> r;
+  if (fixed) {
+    const CRadices c = c_radices(L, true);
+    return std::vector<int>(c.r, c.r + c.n);
+  }
   int m = L;
   if (r16)
     while (m % 16 == 0) { r.push_back(16); m /= 16; }
@@ -112,10 +117,10 @@ static std::vector<int> line_radices(int L, bool r16) {
 
 // Fills the line FFT of length L; returns the twiddle entries it needs and
 // appends their table segments (offsets relative to the shape's table).
-static void make_line(FLine& ln, int L, std::vector<RootSeg>* segs, i64 base, bool r16) {
+static void make_line(FLine& ln, int L, std::vector<RootSeg>* segs, i64 base, bool r16, bool fixed = false) {
   memset(&ln, 0, sizeof ln);
   ln.L = L;
-  const std::vector<int> rs = line_radices(L, r16);
+  const std::vector<int> rs = line_radices(L, r16, fixed);
   if ((int)rs.size() > AFF_MAXPASS) throw FastError("too many passes");
   int p = 1, tw = 0;
   ln.npass = (int)rs.size();
@@ -234,7 +239,7 @@ static void choose_vectors(FShape& s, bool balance) {
     const i64 r1 = (u1 + kThreads - 1) / kThreads;
     const i64 r2 = (u1 / 2 + kThreads - 1) / kThreads;
     // a two-line unit costs about 1.7 one-line units
-    ps.V = (s.GL >= 2 && ps.R != 16 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
+    ps.V = (s.GL >= 2 && ps.R <= 8 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
     ps.glog = ilog2_up(s.GL / ps.V);
   }
 }
@@ -299,7 +304,9 @@ static int line_shape(FastBatch* B, int L) {
   s.Q = 1;
   s.GL = GL;
   const i64 tw_base = B->tab_elems;
-  make_line(s.line, L, &B->segs, tw_base, B->tune.radix16 != 0);
+  // a compile-time line takes its two listed radices (finish_shape marks it)
+  const bool fixed = B->tune.fixed && B->tune.radix16 && !B->tune.balance_v && is_fixed_line(L, GL);
+  make_line(s.line, L, &B->segs, tw_base, B->tune.radix16 != 0, fixed);
   B->tab_elems += s.line.twn;
   finish_shape(s, B->tune);
   B->shapes.push_back(s);
