@@ -246,6 +246,37 @@ struct Sink {
   }
 };
 
+// A store phase over the u = tid, tid + T, ... < total elements of a tile:
+// idx(u) gives element u's output offset from `base` (< 0: none), val(u) its
+// value; the weights of the cotangent epilogue are loaded four elements at a
+// time before the values are formed, so that their latency is paid once per
+// four.
+template <int T, class Idx, class Val>
+AF_HD void store_phase(int tid, int total, const Sink& sk, i64 base, Idx idx, Val val, float& loss) {
+  const float* w = sk.w ? sk.w + base : nullptr;
+  cx* out = sk.out + base;
+  for (int u0 = tid; u0 < total; u0 += 4 * T) {
+    int o[4];
+    float wt[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int u = u0 + r * T;
+      o[r] = u < total ? idx(u) : -1;
+      wt[r] = (w && o[r] >= 0) ? ldf(w + o[r]) : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (o[r] >= 0) {
+        cx t = val(u0 + r * T);
+        if (w) {
+          loss += wt[r] * (t.x * t.x + t.y * t.y);
+          t = cscale(t, 2.f * wt[r]);
+        }
+        out[o[r]] = t;
+      }
+  }
+}
+
 // workspace element written by another CTA of this launch: read at L2 (no
 // stale L1 line)
 AF_HD cx ldws(const cx* p) {
@@ -643,10 +674,13 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
-    for (int u = tid; u < L * GL; u += T) {
-      const int k2 = u >> glogR, l = u & (GL - 1);
-      if (l < cn) sk.put(x.off + c0 + l + (i64)n1 * k2, res[lpos(k2, l, S.LS)], loss);
-    }
+    store_phase<T>(
+        tid, L * GL, sk, x.off,
+        [&](int u) {
+          const int k2 = u >> glogR, l = u & (GL - 1);
+          return l < cn ? c0 + l + n1 * k2 : -1;
+        },
+        [&](int u) { return res[lpos(u >> glogR, u & (GL - 1), S.LS)]; }, loss);
   });
 }
 
@@ -721,12 +755,17 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
-    for (int u = tid; u < L * GL; u += T) {
-      const int j1 = u >> glogC, c = u & (GL - 1);
-      const int j = j1 * M2 + c0 + c;
-      if (c < cn && j < x.n)
-        sk.put(x.off + j, cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j)), loss);
-    }
+    store_phase<T>(
+        tid, L * GL, sk, x.off,
+        [&](int u) {
+          const int c = u & (GL - 1), j = (u >> glogC) * M2 + c0 + c;
+          return c < cn && j < x.n ? j : -1;
+        },
+        [&](int u) {
+          const int j1 = u >> glogC, c = u & (GL - 1);
+          return cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j1 * M2 + c0 + c));
+        },
+        loss);
   });
 }
 
