@@ -99,7 +99,19 @@ struct DevExec {
   unsigned par = 0;  // parity of the mbarrier phase the next bulk copy completes
   unsigned* err = nullptr;  // the launch's error word
   bool failed = false;      // a bulk copy of this CTA timed out (uniform after the phase's barrier)
+  unsigned* head = nullptr;  // the queue head (null: no claims)
+  int nxt = 0;               // thread 0: the item claimed for the CTA's next round
+  const FItem* items = nullptr;
+  int nitems = 0;
 #ifdef __CUDACC__
+  // Thread 0 claims the CTA's next item at the start of an item's load
+  // phase, and copies that item's record into s_itn with the phase's
+  // asynchronous copies: the claim's and the record's round trips overlap the
+  // load instead of delaying the top of the next round.
+  __device__ __forceinline__ void claim() {
+    if (head && threadIdx.x == 0) nxt = (int)atomicAdd(head, 1u);
+  }
+  __device__ __forceinline__ void prefetch_next();
   template <class F>
   __device__ __forceinline__ void phase(F&& f) {
     f((int)threadIdx.x);
@@ -117,6 +129,7 @@ struct DevExec {
   __device__ __forceinline__ void phase_load(F&& f, cx* dst, const cx* src, unsigned bytes, const cx* drop,
                                              i64 drop_elems) {
     const unsigned mb = smem_u32(&s_mbar);
+    claim();
     if (threadIdx.x == 0) {
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
@@ -126,6 +139,7 @@ struct DevExec {
                    : "memory");
     }
     f((int)threadIdx.x);
+    prefetch_next();
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     unsigned done = 0;
@@ -142,7 +156,9 @@ struct DevExec {
   }
   template <class F>
   __device__ __forceinline__ void phase_async(F&& f) {
+    claim();
     f((int)threadIdx.x);
+    prefetch_next();
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
@@ -304,11 +320,23 @@ AF_HD cx tl3(const cx* tab, unsigned t) {
   }
   return cmul(cmul(c, b), a);
 }
+// m^2 mod N for m^2 / N < 2^21 (the planner keeps N = 2n <= 2^18, m < n):
+// the float estimate m m (1/N) of the quotient is within 3 * 2^-24 of it
+// relatively, so off by at most one; the remainder, exact modulo 2^32, is
+// then corrected once either way.
+AF_HD unsigned sqmod(unsigned m, unsigned N, float rN) {
+  const float fm = (float)m;
+  const unsigned q = (unsigned)(fm * fm * rN);
+  int r = (int)(m * m - q * N);
+  if (r < 0) r += (int)N;
+  if (r >= (int)N) r -= (int)N;
+  return (unsigned)r;
+}
 // Bluestein chirp a_m = W_{2n}^(m^2 mod 2n) (forward root; the exact index
 // keeps the phase of large m accurate); ct is the three-level table of W_{2n}
 template <bool GLOBAL>
 AF_HD cx chirp_at(const FXform& x, const cx* ct, int m) {
-  return tl3<GLOBAL>(ct, mulmod((unsigned)m, (unsigned)m, x.mod2n));
+  return tl3<GLOBAL>(ct, sqmod((unsigned)m, x.n2x, x.r2n));
 }
 // Bluestein spectrum entry k of M: the spectrum of the even chirp is even,
 // so only entries 0..M/2 are stored
@@ -393,7 +421,17 @@ extern __shared__ float4 fsm4[];
 __shared__ FShape s_shape;
 __shared__ FXform s_xf[AFF_MAXQ];
 __shared__ FItem s_it;
+__shared__ __align__(16) FItem s_itn;  // the record of the claimed next item
 __shared__ int s_item, s_ok;
+__device__ __forceinline__ void DevExec::prefetch_next() {
+  static_assert(sizeof(FItem) % 16 == 0, "item records move as 16-byte copies");
+  if (head && threadIdx.x == 0 && nxt < nitems) {
+    const cx* src = reinterpret_cast<const cx*>(items + nxt);
+    cx* dst = reinterpret_cast<cx*>(&s_itn);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(FItem) / 16); ++k) cp_async16(dst + 2 * k, src + 2 * k);
+  }
+}
 
 // One out-of-line copy of the line FFT per sign, shared by every item kind
 // (keeps the kernel's code, and its compile time, small); its buffers are
@@ -803,8 +841,8 @@ __device__ __forceinline__ void copy_words(void* dst, const void* src, int n) {
 // Persistent executor: every CTA takes the next item of the queue (items
 // wait only for items earlier in the queue, and the smallest unfinished item
 // is always held by a CTA that has started it or is about to, so the launch
-// always completes).  Thread 0 claims the CTA's following item while the
-// current one runs.  A wait polls its counter at most spin_limit times; then
+// always completes).  Thread 0 claims the CTA's following item in the
+// current item's load phase.  A wait polls its counter at most spin_limit times; then
 // the CTA records FE_TIMEOUT and leaves, and the items that depend on it
 // time out in turn.  The item's shape and transforms are staged in shared
 // memory (the shape only when it changes).
@@ -813,20 +851,23 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
                                                               long long spin_limit) {
   DevExec ex;
   ex.err = ctrs;
+  ex.head = ctrs + FC_HEAD;
+  ex.items = A.items;
+  ex.nitems = nitems;
   int loaded = -1;  // shape staged in s_shape (uniform across the CTA)
-  int next = 0;     // thread 0: the item claimed for the next round
   if (threadIdx.x == 0) {
-    next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+    ex.nxt = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+    if (ex.nxt < nitems) s_itn = A.items[ex.nxt];
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
   for (;;) {
     if (threadIdx.x == 0) {
-      const int i = next;
+      const int i = ex.nxt;
       int ok = 1;
       if (i < nitems) {
-        const FItem it = A.items[i];
+        const FItem it = s_itn;
         s_it = it;
         if (it.wait_ctr >= 0) {
           long long k = 0;
@@ -839,7 +880,6 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
             __nanosleep(64);
           }
         }
-        if (ok) next = (int)atomicAdd(ctrs + FC_HEAD, 1u);
       }
       s_item = i;
       s_ok = ok;
@@ -858,12 +898,10 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
     if (ex.failed) break;
     if (it.done_ctr >= 0) {
       // every thread's stores of this item precede the barrier; thread 0's
-      // fence then publishes them before the count
+      // release increment then publishes them with the count
       __syncthreads();
-      if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(ctrs + it.done_ctr, 1u);
-      }
+      if (threadIdx.x == 0)
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctrs + it.done_ctr) : "memory");
     }
   }
   if (A.w && A.loss) {

@@ -49,6 +49,7 @@ struct FItem {
   int c0, cn;                     // multi-pass items: columns or lines [c0, c0 + cn)
   int wait_ctr, wait_cnt;         // start once counter wait_ctr reaches wait_cnt (-1: no wait)
   int done_ctr;                   // counter this item increments when done (-1: none)
+  int pad[3];                     // 48 bytes: the kernel prefetches an item with 16-byte copies
 };
 
 // Counters of a persistent launch: the queue head, the error word, then the
@@ -69,7 +70,8 @@ struct FXform {
   const cx* ct;    // Bluestein: three-level table of W_{2n} (chirp a_m = W_{2n}^(m^2))
   const cx* wt;    // multi-pass: three-level table of W_n (direct) or W_M (Bluestein)
   const cx* spec;  // Bluestein: spectrum FFT(b)/M of the conjugate chirp, entries 0..M/2
-  ModN mod2n;      // reduction mod 2n
+  unsigned n2x;    // Bluestein: 2n, the chirp's modulus
+  float r2n;       // Bluestein: 1 / (2n) rounded to float
 };
 
 struct FArgs {

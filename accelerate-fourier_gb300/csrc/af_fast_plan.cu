@@ -482,7 +482,7 @@ static void plan_batch(FastBatch* B) {
       Q *= 2;
     const int si = full_shape(B, kind, len, Q);
     for (size_t j = 0; j < idx.size(); j += Q) {
-      FItem it;
+      FItem it{};
       memset(&it, 0, sizeof it);
       it.kind = kind;
       it.shape = si;
@@ -496,7 +496,8 @@ static void plan_batch(FastBatch* B) {
         i64 ct = -1, spec = -1;
         if (kind == FK_BLUE) {
           x.M = (int)len;
-          x.mod2n = make_modn((unsigned long long)(2 * n));
+          x.n2x = (unsigned)(2 * n);
+          x.r2n = 1.0f / (float)(2 * n);
           ct = table_tl3(B, 2 * n);
           spec = spectrum(B, n, len);
         }
@@ -538,7 +539,8 @@ static void plan_batch(FastBatch* B) {
     i64 ct = -1, spec = -1;
     const i64 wt = table_tl3(B, N);
     if (blue) {
-      x.mod2n = make_modn((unsigned long long)(2 * n));
+      x.n2x = (unsigned)(2 * n);
+      x.r2n = 1.0f / (float)(2 * n);
       ct = table_tl3(B, 2 * n);
       spec = spectrum(B, n, N);
     }
@@ -549,7 +551,7 @@ static void plan_batch(FastBatch* B) {
     auto items = [&](int kind, int si, int C, i64 count) {
       std::vector<FItem> v;
       for (i64 c0 = 0; c0 < count; c0 += C) {
-        FItem it;
+        FItem it{};
         memset(&it, 0, sizeof it);
         it.kind = kind;
         it.shape = si;
