@@ -254,13 +254,15 @@ class BatchRunner:
     every signal with the fused epilogue g = 2 w X, loss = sum w |X|^2) and
     af_batch_vjp (grad = DFT^H g)."""
 
-    def __init__(self, ns, tune=True):
+    def __init__(self, ns, tune=True, cache=None):
         import tempfile
         from accelerate_fourier import _lib
         t0 = time.perf_counter()
         # planner choices timed on this GPU (af_batch_create_tuned); the cache
-        # lives in a fresh temporary file, so every run tunes
-        cache = os.path.join(tempfile.mkdtemp(prefix="af_tune_"), "tune.jsonl") if tune else None
+        # lives in a fresh temporary file, so every run tunes, unless a cache
+        # file is given (profiling runs reuse the choice of an earlier run)
+        if tune and not cache:
+            cache = os.path.join(tempfile.mkdtemp(prefix="af_tune_"), "tune.jsonl")
         self.batch = _lib.Batch(ns, -1, tune=tune, tune_cache=cache)
         self.create_s = time.perf_counter() - t0
         self.describe = self.batch.describe()
@@ -382,7 +384,7 @@ def run_ours(args):
     grad = torch.empty_like(x)
     loss = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    runner = BatchRunner(ns)
+    runner = BatchRunner(ns, cache=args.tune_cache)
 
     def step():
         runner.step(x, w, cot, grad, loss, torch.cuda.current_stream().cuda_stream)
@@ -810,6 +812,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true", help="skip the plain-path comparison (profiling runs)")
     ap.add_argument("--count", type=int, default=COUNT, help="transforms in the workload (profiling runs use fewer)")
+    ap.add_argument("--tune-cache", default="", help="planner-choice cache file to reuse (profiling runs: no tuning "
+                    "launches once an earlier run with the same file has tuned)")
     ap.add_argument("--lengths", default="", help='profiling cases: "n*count,..." in place of the workload')
     ap.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5],
                     help="4: the batched mixed-size headline (default); 1, 2, 3, 5: the other configurations")

@@ -165,8 +165,8 @@ def test_cyclic_reverse_and_scale_exact():
 def test_config2_single_transforms(n):
     """Batch 1, re/im i.i.d. N(0,1), seed 2: 2^20, 3^12, 1001*1024, 65537
     (Rader), 1000003 (the planner picks Bluestein, pad 2025000).  Bound:
-    rel-L2 <= 4 eps32 log2 N against the FP64 oracle; max-abs error <= 8 eps32
-    log2 N times the largest output magnitude."""
+    rel-L2 <= 4 eps32 log2 N and <= 1e-6 against the FP64 oracle; max-abs
+    error <= 8 eps32 log2 N times the largest output magnitude."""
     from accelerate_fourier import planned
     rng = np.random.default_rng(2)
     x = crand(rng, (1, n), "normal")
@@ -179,4 +179,6 @@ def test_config2_single_transforms(n):
     # reference does (k^2 up to 1e12): about 2e-10 from numpy at N = 1000003
     assert rel_l2(ref, np.fft.fft(x, axis=-1)) <= (1e-9 if n == 1000003 else 1e-12)
     assert rel_l2(y, ref) <= fp32_bound(n, 4.0)
+    # the benchmark's acceptance bound for these sizes (measured: 2e-7 to 3e-7)
+    assert rel_l2(y, ref) <= 1e-6
     assert np.abs(y - ref).max() <= 8 * 2.0 ** -24 * np.log2(n) * np.abs(ref).max()
