@@ -108,9 +108,7 @@ struct DevExec {
   // phase, and copies that item's record into s_itn with the phase's
   // asynchronous copies: the claim's and the record's round trips overlap the
   // load instead of delaying the top of the next round.
-  __device__ __forceinline__ void claim() {
-    if (head && threadIdx.x == 0) nxt = (int)atomicAdd(head, 1u);
-  }
+  __device__ __forceinline__ void claim();
   __device__ __forceinline__ void prefetch_next();
   template <class F>
   __device__ __forceinline__ void phase(F&& f) {
@@ -338,10 +336,6 @@ template <bool GLOBAL>
 AF_HD cx chirp_at(const FXform& x, const cx* ct, int m) {
   return tl3<GLOBAL>(ct, sqmod((unsigned)m, x.n2x, x.r2n));
 }
-// Bluestein spectrum entry k of M: the spectrum of the even chirp is even,
-// so only entries 0..M/2 are stored
-AF_HD cx spec_at(const cx* spec, int M, int k) { return ldcx(spec + (2 * k <= M ? k : M - k)); }
-AF_HD cx conjc(cx a) { return make_cx(a.x, -a.y); }
 
 // The radix-G pass over `cnt` transforms of a full-FFT shape: element k1 of
 // line l of transform q at src[(q G + l) LS + k1].  Per unit the sink gives
@@ -384,14 +378,16 @@ AF_HD void final_any(int tid, int T, int cnt, const FShape& S, const cx* src, in
 // Every Stockham pass of the shape's line FFT, ping-ponging between the two
 // buffers; returns the buffer holding the result (line-major, stride S.LS).
 // Each pass moves V lines per unit (its own choice, see FPass).
+// `ep` is the last pass's epilogue (compile-time lines only; the callers
+// pass EPI_PLAIN for the others).
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
+AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw, const LineEpi& ep) {
   if (S.fixed) {  // a compile-time line (the planner sets `fixed` only for listed pairs)
     switch (S.line.L * 1024 + S.GL) {
 #define AFF_FIXED_CASE(L, GL, R1, R2)                      \
   case L * 1024 + GL:                                      \
-    cline_passes<T, SIGN, L, GL, 0>(ex, src, dst, tw);     \
+    cline_passes<T, SIGN, L, GL, 0>(ex, src, dst, tw, ep); \
     return src;
       AFF_FIXED_LINES(AFF_FIXED_CASE)
 #undef AFF_FIXED_CASE
@@ -420,9 +416,17 @@ AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw) {
 extern __shared__ float4 fsm4[];
 __shared__ FShape s_shape;
 __shared__ FXform s_xf[AFF_MAXQ];
-__shared__ FItem s_it;
+__shared__ FItem s_it;                 // the current item's record
 __shared__ __align__(16) FItem s_itn;  // the record of the claimed next item
-__shared__ int s_item, s_ok;
+__shared__ int s_nxt, s_ok;            // the claimed next item's index; its wait succeeded
+// thread 0 claims the CTA's next item; every thread reads s_nxt after the
+// phase's closing barrier
+__device__ __forceinline__ void DevExec::claim() {
+  if (head && threadIdx.x == 0) {
+    nxt = (int)atomicAdd(head, 1u);
+    s_nxt = nxt;
+  }
+}
 __device__ __forceinline__ void DevExec::prefetch_next() {
   static_assert(sizeof(FItem) % 16 == 0, "item records move as 16-byte copies");
   if (head && threadIdx.x == 0 && nxt < nitems) {
@@ -437,21 +441,23 @@ __device__ __forceinline__ void DevExec::prefetch_next() {
 // (keeps the kernel's code, and its compile time, small); its buffers are
 // element offsets into the dynamic shared area.
 template <int T, int SIGN>
-__device__ __noinline__ int line_fft_dev(int so, int doff, int toff) {
+__device__ __noinline__ int line_fft_dev(int so, int doff, int toff, LineEpi ep) {
   DevExec ex;
   cx* base = reinterpret_cast<cx*>(fsm4);
-  cx* r = line_fft<T, SIGN>(ex, s_shape, base + so, base + doff, base + toff);
+  cx* r = line_fft<T, SIGN>(ex, s_shape, base + so, base + doff, base + toff, ep);
   return (int)(r - base);
 }
 template <int T, int SIGN>
-__device__ __forceinline__ cx* run_line(DevExec&, const FShape&, cx* sm, cx* src, cx* dst, const cx* tw) {
-  return sm + line_fft_dev<T, SIGN>((int)(src - sm), (int)(dst - sm), (int)(tw - sm));
+__device__ __forceinline__ cx* run_line(DevExec&, const FShape&, cx* sm, cx* src, cx* dst, const cx* tw,
+                                        const LineEpi& ep = LineEpi{EPI_PLAIN, 0, 0, 0, 0, nullptr}) {
+  return sm + line_fft_dev<T, SIGN>((int)(src - sm), (int)(dst - sm), (int)(tw - sm), ep);
 }
 #endif
 // the emulator runs the line FFT inline
 template <int T, int SIGN>
-cx* run_line(HostExec& ex, const FShape& S, cx*, cx* src, cx* dst, const cx* tw) {
-  return line_fft<T, SIGN>(ex, S, src, dst, tw);
+cx* run_line(HostExec& ex, const FShape& S, cx*, cx* src, cx* dst, const cx* tw,
+             const LineEpi& ep = LineEpi{EPI_PLAIN, 0, 0, 0, 0, nullptr}) {
+  return line_fft<T, SIGN>(ex, S, src, dst, tw, ep);
 }
 
 // shared-memory areas of an item: the two data buffers, the pass twiddles,
@@ -722,23 +728,14 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
   });
 }
 
-// FK_BROWS (Bluestein pass R): lines k1 in [c0, c0 + cn), element j2 at
-// ws[j2 M1 + k1]; FFT_M2; times the spectrum at k1 + M1 k2 and conjugated;
-// FFT_M2 again; twiddle W_M^(j2 k1); stored line-contiguous in the
-// transform's second workspace region: ws[M + k1 M2 + j2] (other items of
-// this pass still read the first).
+// The two row FFTs of a Bluestein row item and the spectrum product between
+// them as a pass of its own (lines that are not compile-time lines); returns
+// the buffer holding the second FFT's result (line-major).
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
-AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
-  const FSmem m = smem_of(S, sm);
-  const FXform& x = xf[0];
+AF_HD cx* brows_spectrum(E& ex, const FShape& S, cx* sm, const FSmem& m, const FXform& x, int c0, int cn) {
   const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
-  const int M1 = x.n1, c0 = it.c0, cn = it.cn;
-  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
-  ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
-                x.s1);
-  if (ex.failed) return;
-  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
+  const int M1 = x.n1;
   cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
   ex.phase([&](int tid) {
@@ -762,7 +759,36 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
       }
     }
   });
-  res = run_line<T, SIGN>(ex, S, sm, nxt, res, m.tw);
+  return run_line<T, SIGN>(ex, S, sm, nxt, res, m.tw);
+}
+
+// FK_BROWS (Bluestein pass R): lines k1 in [c0, c0 + cn), element j2 at
+// ws[j2 M1 + k1]; FFT_M2; times the spectrum at k1 + M1 k2 and conjugated;
+// FFT_M2 again; twiddle W_M^(j2 k1); stored line-contiguous in the
+// transform's second workspace region: ws[M + k1 M2 + j2] (other items of
+// this pass still read the first).
+#pragma nv_exec_check_disable
+template <int T, int SIGN, class E>
+AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
+  const FSmem m = smem_of(S, sm);
+  const FXform& x = xf[0];
+  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int M1 = x.n1, c0 = it.c0, cn = it.cn;
+  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
+  ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
+                x.s1);
+  if (ex.failed) return;
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
+  cx* res;
+  if (S.fixed) {
+    // the spectrum product in the first FFT's last pass, written in the
+    // second FFT's input layout
+    const LineEpi ep{EPI_SPEC, c0, cn, M1, x.M, x.spec};
+    cx* nxt = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw, ep);
+    res = run_line<T, SIGN>(ex, S, sm, nxt, nxt == m.a ? m.b : m.a, m.tw);
+  } else {
+    res = brows_spectrum<T, SIGN>(ex, S, sm, m, x, c0, cn);
+  }
   const int lga = ilog2i(x.ga);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
@@ -830,11 +856,11 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-// n 4-byte words from global to shared memory
-__device__ __forceinline__ void copy_words(void* dst, const void* src, int n) {
+// n 4-byte words from global to shared memory, by the threads of warps 1..
+__device__ __forceinline__ void copy_words32(void* dst, const void* src, int n) {
   const unsigned* s = reinterpret_cast<const unsigned*>(src);
   unsigned* d = reinterpret_cast<unsigned*>(dst);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = __ldg(s + i);
+  for (int i = threadIdx.x - 32; i < n; i += blockDim.x - 32) d[i] = __ldg(s + i);
 }
 #endif
 
@@ -857,40 +883,43 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
   int loaded = -1;  // shape staged in s_shape (uniform across the CTA)
   if (threadIdx.x == 0) {
     ex.nxt = (int)atomicAdd(ctrs + FC_HEAD, 1u);
+    s_nxt = ex.nxt;
     if (ex.nxt < nitems) s_itn = A.items[ex.nxt];
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
   for (;;) {
+    // The claimed item (index and record staged in shared memory by thread 0
+    // during the previous item's load phase, visible after its barriers).
+    // Thread 0 waits for the item's stage counter while the other warps stage
+    // its shape and transforms: the descriptors never change during the
+    // launch, only the workspace the wait guards.
+    if (s_nxt >= nitems) break;
     if (threadIdx.x == 0) {
-      const int i = ex.nxt;
+      const FItem it = s_itn;
+      s_it = it;
       int ok = 1;
-      if (i < nitems) {
-        const FItem it = s_itn;
-        s_it = it;
-        if (it.wait_ctr >= 0) {
-          long long k = 0;
-          while (ld_acquire(ctrs + it.wait_ctr) < (unsigned)it.wait_cnt) {
-            if (++k > spin_limit) {
-              atomicExch(ctrs + FC_ERROR, (unsigned)FE_TIMEOUT);
-              ok = 0;
-              break;
-            }
-            __nanosleep(64);
+      if (it.wait_ctr >= 0) {
+        long long k = 0;
+        while (ld_acquire(ctrs + it.wait_ctr) < (unsigned)it.wait_cnt) {
+          if (++k > spin_limit) {
+            atomicExch(ctrs + FC_ERROR, (unsigned)FE_TIMEOUT);
+            ok = 0;
+            break;
           }
+          __nanosleep(64);
         }
       }
-      s_item = i;
       s_ok = ok;
+    } else if (threadIdx.x >= 32) {
+      const int shape = s_itn.shape;
+      if (shape != loaded) copy_words32(&s_shape, A.shapes + shape, (int)(sizeof(FShape) / 4));
+      copy_words32(s_xf, A.xf + s_itn.first, s_itn.count * (int)(sizeof(FXform) / 4));
     }
     __syncthreads();
-    const int i = s_item;
-    if (i >= nitems || !s_ok) break;
+    if (!s_ok) break;
     const FItem it = s_it;
-    if (it.shape != loaded) copy_words(&s_shape, A.shapes + it.shape, (int)(sizeof(FShape) / 4));
-    copy_words(s_xf, A.xf + it.first, it.count * (int)(sizeof(FXform) / 4));
-    __syncthreads();
     loaded = it.shape;
     run_item<T, SIGN>(ex, A, it, s_shape, s_xf, reinterpret_cast<cx*>(fsm4));
     // a bulk copy that never completed: this CTA takes no further items (the

@@ -72,6 +72,24 @@ AF_HD cx cmul_s(cx a, cx w) {
   return make_cx(rfma(a.x, w.x, a.y * w.y), rfma(a.y, w.x, -a.x * w.y));
 }
 
+AF_HD cx conjc(cx a) { return make_cx(a.x, -a.y); }
+// Bluestein spectrum entry k of M: the spectrum of the even chirp is even,
+// so only entries 0..M/2 are stored
+AF_HD cx spec_at(const cx* spec, int M, int k) { return ldcx(spec + (2 * k <= M ? k : M - k)); }
+
+// What the last pass of a compile-time line does with its outputs.
+// EPI_PLAIN: writes them line-major (stride L | 1).  EPI_SPEC (the first row
+// FFT of a Bluestein row item): output e of line l becomes
+// conj(y * spec[c0 + l + M1 e]) for l < cn, zero for the lines past cn, and
+// is written interleaved (e GL + l), the layout the second row FFT reads, so
+// that the spectrum product needs no pass of its own.
+enum { EPI_PLAIN = 0, EPI_SPEC = 1 };
+struct LineEpi {
+  int mode;
+  int c0, cn, M1, M;
+  const cx* spec;
+};
+
 template <int V> struct FVec;
 template <> struct FVec<1> {
   typedef float2 T;
@@ -271,28 +289,81 @@ AF_HD void cpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, int b, i
   }
 }
 
+// The last pass of a compile-time line with the EPI_SPEC epilogue (the last
+// pass has P = NB, so butterfly b is k = b and its outputs are e = k + m P).
+template <int R, int V, int SIGN, int P, int NB, int GL>
+AF_HD void cpass_unit_spec(const cx* __restrict__ src, cx* __restrict__ dst, int b, int line,
+                           const cx* __restrict__ tw, const LineEpi& ep) {
+  static_assert(P == NB, "the spectrum epilogue belongs to the last pass");
+  cx a[V][R];
+  const int ib = b * GL + line;
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    cx t[V];
+    FVec<V>::get(src + ib + m * (NB * GL), t);
+#pragma unroll
+    for (int v = 0; v < V; ++v) a[v][m] = t[v];
+  }
+  if (P > 1 && b > 0) {
+#pragma unroll
+    for (int m = 1; m < R; ++m) {
+      const cx w = tw[(m - 1) * P + b];
+#pragma unroll
+      for (int v = 0; v < V; ++v) a[v][m] = cmul_s<SIGN>(a[v][m], w);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) Dft<R>::run(a[v], (rl)SIGN, nullptr, 0, 0);
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    const int e = b + m * P;
+    cx t[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int l = line + v;
+      t[v] = l < ep.cn ? conjc(cmul_s<SIGN>(a[v][m], spec_at(ep.spec, ep.M, ep.c0 + l + ep.M1 * e)))
+                       : make_cx(0.f, 0.f);
+    }
+    FVec<V>::put(dst + e * GL + line, t);
+  }
+}
+
 template <int T, int R, int V, int SIGN, int P, int NB, int GL, int LS>
 AF_HD void cpass_thread(int tid, const cx* src, cx* dst, const cx* tw) {
   constexpr int per = GL / V, units = NB * per;
   for (int u = tid; u < units; u += T) cpass_unit<R, V, SIGN, P, NB, GL, LS>(src, dst, u / per, (u % per) * V, tw);
 }
 
-// Passes J.. of the compile-time line (L, GL); src and dst swap after each.
+// Passes J.. of the compile-time line (L, GL); src and dst swap after each;
+// the last pass ends with the epilogue `ep`.
 #pragma nv_exec_check_disable
 template <int T, int SIGN, int L, int GL, int J, class E>
-AF_HD void cline_passes(E& ex, cx*& src, cx*& dst, const cx* tw) {
+AF_HD void cline_passes(E& ex, cx*& src, cx*& dst, const cx* tw, const LineEpi& ep) {
   constexpr CRadices rs = c_radices(L);
   if constexpr (J < rs.n) {
     constexpr int R = rs.r[J], P = c_span(L, J), NB = L / R;
     constexpr int V = (GL >= 2 && R <= 8) ? 2 : 1;
-    constexpr int LSo = J == rs.n - 1 ? (L | 1) : 0;
+    constexpr bool LAST = J == rs.n - 1;
+    constexpr int LSo = LAST ? (L | 1) : 0;
     constexpr int TW = c_twoff(L, J);
     cx* s = src;
     cx* d = dst;
-    ex.phase([&](int tid) { cpass_thread<T, R, V, SIGN, P, NB, GL, LSo>(tid, s, d, tw + TW); });
+    if constexpr (LAST) {
+      if (ep.mode == EPI_SPEC) {
+        ex.phase([&](int tid) {
+          constexpr int per = GL / V, units = NB * per;
+          for (int u = tid; u < units; u += T)
+            cpass_unit_spec<R, V, SIGN, P, NB, GL>(s, d, u / per, (u % per) * V, tw + TW, ep);
+        });
+      } else {
+        ex.phase([&](int tid) { cpass_thread<T, R, V, SIGN, P, NB, GL, LSo>(tid, s, d, tw + TW); });
+      }
+    } else {
+      ex.phase([&](int tid) { cpass_thread<T, R, V, SIGN, P, NB, GL, LSo>(tid, s, d, tw + TW); });
+    }
     src = d;
     dst = s;
-    cline_passes<T, SIGN, L, GL, J + 1>(ex, src, dst, tw);
+    cline_passes<T, SIGN, L, GL, J + 1>(ex, src, dst, tw, ep);
   }
 }
 
