@@ -101,14 +101,18 @@ struct DevExec {
   bool failed = false;      // a bulk copy of this CTA timed out (uniform after the phase's barrier)
   unsigned* head = nullptr;  // the queue head (null: no claims)
   int nxt = 0;               // thread 0: the item claimed for the CTA's next round
+  int ahead = 0;             // thread 0, during a load phase: the item claimed for the round after
   const FItem* items = nullptr;
   int nitems = 0;
 #ifdef __CUDACC__
-  // Thread 0 claims the CTA's next item at the start of an item's load
-  // phase, and copies that item's record into s_itn with the phase's
-  // asynchronous copies: the claim's and the record's round trips overlap the
-  // load instead of delaying the top of the next round.
+  // The CTA claims its items two rounds ahead.  At the start of an item's
+  // load phase thread 0 takes the next item (claimed one round earlier),
+  // copies its record into s_itn with the phase's asynchronous copies, and
+  // claims the item after it; publish() hands both to the CTA at the end of
+  // the phase.  Neither round trip delays the phase: the record's address is
+  // known at once, and the claim's result is needed only at the phase's end.
   __device__ __forceinline__ void claim();
+  __device__ __forceinline__ void publish();
   __device__ __forceinline__ void prefetch_next();
   template <class F>
   __device__ __forceinline__ void phase(F&& f) {
@@ -147,6 +151,7 @@ struct DevExec {
                    : "r"(mb), "r"(par)
                    : "memory");
     par ^= 1u;
+    publish();
     if (!done) atomicExch(err + FC_ERROR, (unsigned)FE_TIMEOUT);
     for (i64 i = 16 * (i64)threadIdx.x; i < drop_elems; i += 16 * (i64)blockDim.x)
       asm volatile("discard.global.L2 [%0], 128;\n" ::"l"(drop + i) : "memory");
@@ -159,6 +164,7 @@ struct DevExec {
     prefetch_next();
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    publish();
     __syncthreads();
   }
   // a phase whose threads accumulate into their own running sum
@@ -419,12 +425,19 @@ __shared__ FXform s_xf[AFF_MAXQ];
 __shared__ FItem s_it;                 // the current item's record
 __shared__ __align__(16) FItem s_itn;  // the record of the claimed next item
 __shared__ int s_nxt, s_ok;            // the claimed next item's index; its wait succeeded
-// thread 0 claims the CTA's next item; every thread reads s_nxt after the
-// phase's closing barrier
+__shared__ int s_ahead;                // the item claimed for the round after the next
+// thread 0 claims for the CTA; every thread reads s_nxt after the phase's
+// closing barrier
 __device__ __forceinline__ void DevExec::claim() {
   if (head && threadIdx.x == 0) {
-    nxt = (int)atomicAdd(head, 1u);
+    nxt = s_ahead;
+    ahead = (int)atomicAdd(head, 1u);
+  }
+}
+__device__ __forceinline__ void DevExec::publish() {
+  if (head && threadIdx.x == 0) {
     s_nxt = nxt;
+    s_ahead = ahead;
   }
 }
 __device__ __forceinline__ void DevExec::prefetch_next() {
@@ -680,8 +693,11 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
     copy_multi_tables(tid, T, S, m, x);
   });
   if (blue) {  // the chirp a_j on the loaded x_j, from the staged table
+    // rows e >= ceil((n - c0) / n2) hold only padding
+    const i64 rr = ((i64)x.n - c0 + n2 - 1) / n2;
+    const int rows = rr < L ? (int)rr : L;
     ex.phase([&](int tid) {
-      for (int i = tid; i < L * GL; i += T) {
+      for (int i = tid; i < rows * GL; i += T) {
         const int e = i >> glogC, c = i & (GL - 1);
         const int j = e * n2 + c0 + c;
         if (c < cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
@@ -867,7 +883,8 @@ __device__ __forceinline__ void copy_words32(void* dst, const void* src, int n) 
 // Persistent executor: every CTA takes the next item of the queue (items
 // wait only for items earlier in the queue, and the smallest unfinished item
 // is always held by a CTA that has started it or is about to, so the launch
-// always completes).  Thread 0 claims the CTA's following item in the
+// always completes, also with each CTA holding the items of its next two
+// rounds: those follow its current one in the queue).  Thread 0 claims in the
 // current item's load phase.  A wait polls its counter at most spin_limit times; then
 // the CTA records FE_TIMEOUT and leaves, and the items that depend on it
 // time out in turn.  The item's shape and transforms are staged in shared
@@ -884,6 +901,7 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
   if (threadIdx.x == 0) {
     ex.nxt = (int)atomicAdd(ctrs + FC_HEAD, 1u);
     s_nxt = ex.nxt;
+    s_ahead = (int)atomicAdd(ctrs + FC_HEAD, 1u);
     if (ex.nxt < nitems) s_itn = A.items[ex.nxt];
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
