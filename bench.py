@@ -86,7 +86,12 @@ def next_prime(n: int) -> int:
     return n
 
 
-def workload_sizes(count: int = COUNT, seed: int = 4):
+CATEGORIES = ("all", "smooth", "prime", "raw")
+
+
+def workload_sizes(count: int = COUNT, seed: int = 4, category: str = "all"):
+    """The workload's lengths; `category` keeps only those drawn as 5-smooth,
+    as the next prime, or left raw (profiling cases: one category's time)."""
     rng = np.random.default_rng(seed)
     base = np.round(np.exp(rng.uniform(math.log(16), math.log(65536), count))).astype(np.int64)
     cat = rng.uniform(size=count)
@@ -99,9 +104,14 @@ def workload_sizes(count: int = COUNT, seed: int = 4):
             lo = sm[max(i - 1, 0)]
             hi = sm[min(i, len(sm) - 1)]
             n = int(lo if (n - lo) <= (hi - n) else hi)
+            kind = "smooth"
         elif c < 0.75:
             n = next_prime(n)
-        out.append(n)
+            kind = "prime"
+        else:
+            kind = "raw"
+        if category in ("all", kind):
+            out.append(n)
     return np.array(out, dtype=np.int64)
 
 
@@ -372,7 +382,7 @@ def dist_setup(torch):
 def run_ours(args):
     import torch
     rank, world, dist = dist_setup(torch)
-    ns = parse_lengths(args.lengths) if args.lengths else workload_sizes(args.count)
+    ns = parse_lengths(args.lengths) if args.lengths else workload_sizes(args.count, category=args.category)
     total = int(ns.sum())
     nbytes = 32 * total
     rng = np.random.default_rng(5)
@@ -490,7 +500,8 @@ def run_ours(args):
     achieved = alg_bytes / ((ms_fwd + ms_vjp) * 1e-3) / 1e9
     # DRAM bytes of one step's persistent launches, from the committed ncu
     # summary (with the commit it was taken at, so that a stale figure shows)
-    traffic, traffic_commit = profiled_traffic() if args.count == COUNT and not args.lengths else (None, None)
+    full = args.count == COUNT and not args.lengths and args.category == "all"
+    traffic, traffic_commit = profiled_traffic() if full else (None, None)
     cpu = None
     if not args.no_cpu and world == 1:
         v, cores, sample = cpu_baseline(ns)
@@ -500,7 +511,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
         "config": {"workload": "4096 mixed-size C2C transforms, n log-uniform [16, 65536] "
-                               "(50% 5-smooth, 25% prime, 25% raw), fwd + cotangent + VJP",
+                               "(50% 5-smooth, 25% prime, 25% raw), fwd + cotangent + VJP"
+                               + ("" if full else f" [profiling case: {args.lengths or args.category}, "
+                                  f"{len(ns)} transforms]"),
                    "sum_n": total, "path": "af_batch_* (one persistent launch per direction), CUDA graph",
                    "parallelism": f"replicas x{world} (no exchange)",
                    "l2": "inputs (267 MB) larger than L2",
@@ -815,6 +828,8 @@ def main():
     ap.add_argument("--tune-cache", default="", help="planner-choice cache file to reuse (profiling runs: no tuning "
                     "launches once an earlier run with the same file has tuned)")
     ap.add_argument("--lengths", default="", help='profiling cases: "n*count,..." in place of the workload')
+    ap.add_argument("--category", default="all", choices=CATEGORIES,
+                    help="profiling cases: only the workload's 5-smooth, prime or raw lengths")
     ap.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5],
                     help="4: the batched mixed-size headline (default); 1, 2, 3, 5: the other configurations")
     args = ap.parse_args()
