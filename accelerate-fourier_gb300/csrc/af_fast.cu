@@ -872,11 +872,11 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-// n 4-byte words from global to shared memory, by the threads of warps 1..
-__device__ __forceinline__ void copy_words32(void* dst, const void* src, int n) {
+// n 4-byte words from global to shared memory, by the threads of warps 2..
+__device__ __forceinline__ void copy_words64(void* dst, const void* src, int n) {
   const unsigned* s = reinterpret_cast<const unsigned*>(src);
   unsigned* d = reinterpret_cast<unsigned*>(dst);
-  for (int i = threadIdx.x - 32; i < n; i += blockDim.x - 32) d[i] = __ldg(s + i);
+  for (int i = threadIdx.x - 64; i < n; i += blockDim.x - 64) d[i] = __ldg(s + i);
 }
 #endif
 
@@ -910,13 +910,15 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
   for (;;) {
     // The claimed item (index and record staged in shared memory by thread 0
     // during the previous item's load phase, visible after its barriers).
-    // Thread 0 waits for the item's stage counter while the other warps stage
-    // its shape and transforms: the descriptors never change during the
-    // launch, only the workspace the wait guards.
+    // Thread 32 waits for the item's stage counter while warps 2.. stage its
+    // shape and transforms (the descriptors never change during the launch,
+    // only the workspace the wait guards) and thread 0 finishes the previous
+    // item's completion count: the three round trips overlap.
     if (s_nxt >= nitems) break;
     if (threadIdx.x == 0) {
+      s_it = s_itn;
+    } else if (threadIdx.x == 32) {
       const FItem it = s_itn;
-      s_it = it;
       int ok = 1;
       if (it.wait_ctr >= 0) {
         long long k = 0;
@@ -930,10 +932,10 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
         }
       }
       s_ok = ok;
-    } else if (threadIdx.x >= 32) {
+    } else if (threadIdx.x >= 64) {
       const int shape = s_itn.shape;
-      if (shape != loaded) copy_words32(&s_shape, A.shapes + shape, (int)(sizeof(FShape) / 4));
-      copy_words32(s_xf, A.xf + s_itn.first, s_itn.count * (int)(sizeof(FXform) / 4));
+      if (shape != loaded) copy_words64(&s_shape, A.shapes + shape, (int)(sizeof(FShape) / 4));
+      copy_words64(s_xf, A.xf + s_itn.first, s_itn.count * (int)(sizeof(FXform) / 4));
     }
     __syncthreads();
     if (!s_ok) break;
@@ -943,13 +945,10 @@ __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitem
     // a bulk copy that never completed: this CTA takes no further items (the
     // items that wait for this one time out in turn)
     if (ex.failed) break;
-    if (it.done_ctr >= 0) {
-      // every thread's stores of this item precede the barrier; thread 0's
-      // release increment then publishes them with the count
-      __syncthreads();
-      if (threadIdx.x == 0)
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctrs + it.done_ctr) : "memory");
-    }
+    // every thread's stores of this item precede the barrier that closed its
+    // last phase; thread 0's release increment publishes them with the count
+    if (it.done_ctr >= 0 && threadIdx.x == 0)
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctrs + it.done_ctr) : "memory");
   }
   if (A.w && A.loss) {
     __syncthreads();
