@@ -885,10 +885,11 @@ __device__ __forceinline__ void copy_words64(void* dst, const void* src, int n) 
 // is always held by a CTA that has started it or is about to, so the launch
 // always completes, also with each CTA holding the items of its next two
 // rounds: those follow its current one in the queue).  Thread 0 claims in the
-// current item's load phase.  A wait polls its counter at most spin_limit times; then
-// the CTA records FE_TIMEOUT and leaves, and the items that depend on it
-// time out in turn.  The item's shape and transforms are staged in shared
-// memory (the shape only when it changes).
+// current item's load phase.  A wait (thread 32, in the item's prologue)
+// polls its counter at most spin_limit times; then the CTA records
+// FE_TIMEOUT and leaves, and the items that depend on it time out in turn.
+// The item's shape and transforms are staged in shared memory (the shape only
+// when it changes).
 template <int T, int SIGN>
 __global__ void __launch_bounds__(T, AFF_MINB(T)) fast_kernel(FArgs A, int nitems, unsigned* ctrs,
                                                               long long spin_limit) {

@@ -33,7 +33,7 @@ struct FastTune {
   int gl_max = 32;          // most lines in one multi-pass item
   int balance_v = 0;        // per-pass choice of lines per unit (else two whenever possible)
   int target = 4096;        // elements one item aims at
-  int slack = 1368;         // items queued between dependent stages (three times the resident CTAs)
+  int slack = 2736;         // items queued between dependent stages (six times the resident CTAs)
   int l2_mb = 48;           // workspace in flight, MB (kept well inside the 126 MB L2)
   int fixed = 1;            // compile-time line FFTs for the listed (L, GL) pairs
 };
@@ -980,7 +980,7 @@ FastBatch* fast_create_tuned(const i64* ns, i64 count, const char* cache_path, c
     const struct {
       int field;
       std::vector<int> values;
-    } axes[] = {{4, {912, 2736}}, {1, {16, 64}}, {0, {0}}, {3, {3072}}};
+    } axes[] = {{4, {1368, 5472}}, {1, {16, 64}}, {0, {0}}, {3, {3072}}};
     for (const auto& ax : axes)
       for (int val : ax.values) {
         int cand[kTuneFields];
