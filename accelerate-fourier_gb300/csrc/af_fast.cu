@@ -297,6 +297,11 @@ AF_HD void store_phase(int tid, int total, const Sink& sk, i64 base, Idx idx, Va
   }
 }
 
+// x / d for 0 <= x < 8192 from r = ceil(2^19 / d), 2 <= d: exact when
+// d <= 64, since then x (r d - 2^19) < 8192 d <= 2^19, and for every power
+// of two (r d = 2^19); x r < 2^31.  One multiply and one shift.
+AF_HD int sdiv(int x, int r) { return (int)(((unsigned)x * (unsigned)r) >> 19); }
+
 // workspace element written by another CTA of this launch: read at L2 (no
 // stale L1 line)
 AF_HD cx ldws(const cx* p) {
@@ -522,15 +527,15 @@ AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
 // no limit on the source positions
 #define kAll ((i64)1 << 62)
 template <bool WS>
-AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, i64 stride, int L, int cn,
+AF_HD void load_lines(int tid, int T, cx* dst, int GL, int gr, const cx* src, i64 stride, int L, int cn,
                       i64 lim) {
   const cx z = make_cx(0.f, 0.f);
-  const bool v16 = GL >= 2 && ((reinterpret_cast<unsigned long long>(src) & 15) == 0) && (stride % 2 == 0) &&
+  const bool v16 = GL % 2 == 0 && ((reinterpret_cast<unsigned long long>(src) & 15) == 0) && (stride % 2 == 0) &&
                    (cn % 2 == 0);
   if (v16) {
-    const int hlog = glog - 1, half = GL >> 1;
+    const int half = GL >> 1;
     for (int i = tid; i < L * half; i += T) {
-      const int e = i >> hlog, c = (i & (half - 1)) * 2;
+      const int e = sdiv(2 * i, gr), c = 2 * i - e * GL;
       cx* d = dst + e * GL + c;
       const i64 s = e * stride + c;
       if (c < cn && s + 1 < lim) {
@@ -546,7 +551,7 @@ AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, 
     }
   } else {
     for (int i = tid; i < L * GL; i += T) {
-      const int e = i >> glog, c = i & (GL - 1);
+      const int e = sdiv(i, gr), c = i - e * GL;
       const i64 s = e * stride + c;
       if (c >= cn || s >= lim) dst[i] = z;
       else if (WS) dst[i] = ldws(src + s);
@@ -559,10 +564,10 @@ AF_HD void load_lines(int tid, int T, cx* dst, int GL, int glog, const cx* src, 
 // holds lines past the transform, which no item writes) set to zero.
 #pragma nv_exec_check_disable
 template <int T, class E>
-AF_HD void zero_lines(E& ex, cx* a, int L, int GL, int cn) {
+AF_HD void zero_lines(E& ex, cx* a, int L, int GL, int gr, int cn) {
   ex.phase([&](int tid) {
     for (int i = tid; i < L * GL; i += T)
-      if ((i & (GL - 1)) >= cn) a[i] = make_cx(0.f, 0.f);
+      if (i - sdiv(i, gr) * GL >= cn) a[i] = make_cx(0.f, 0.f);
   });
 }
 
@@ -685,11 +690,11 @@ template <int T, int SIGN, class E>
 AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm, bool blue) {
   const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int L = S.line.L, GL = S.GL;
   const int n2 = x.n2, c0 = it.c0, cn = it.cn;
   ex.phase_async([&](int tid) {
     // FK_BCOLS: x zero padded past n (natural index j = e n2 + c0 + c)
-    load_lines<false>(tid, T, m.a, GL, glogC, A.in + x.off + c0, n2, L, cn, blue ? (i64)x.n - c0 : kAll);
+    load_lines<false>(tid, T, m.a, GL, S.GLr, A.in + x.off + c0, n2, L, cn, blue ? (i64)x.n - c0 : kAll);
     copy_multi_tables(tid, T, S, m, x);
   });
   if (blue) {  // the chirp a_j on the loaded x_j, from the staged table
@@ -698,21 +703,21 @@ AF_HD void cols_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
     const int rows = rr < L ? (int)rr : L;
     ex.phase([&](int tid) {
       for (int i = tid; i < rows * GL; i += T) {
-        const int e = i >> glogC, c = i & (GL - 1);
+        const int e = sdiv(i, S.GLr), c = i - e * GL;
         const int j = e * n2 + c0 + c;
         if (c < cn && j < x.n) m.a[i] = cmul_s<SIGN>(m.a[i], chirp_at<false>(x, m.ct3, j));
       }
     });
   }
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
-  const int lgb = ilog2i(x.gb);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int c = (int)fdiv((unsigned)u, S.L1div);
       const int k1 = u - c * L;
       const int j2 = c0 + c;
       const cx v = cmul_s<SIGN>(res[lpos(k1, c, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
-      A.ws[x.ws + (i64)(k1 >> lgb) * x.s1 + j2 * x.gb + (k1 & (x.gb - 1))] = v;  // block k1 / gb
+      const int kb = sdiv(k1, x.gbr);
+      A.ws[x.ws + (i64)kb * x.s1 + j2 * x.gb + (k1 - kb * x.gb)] = v;  // block k1 / gb
     }
   });
 }
@@ -724,23 +729,27 @@ template <int T, int SIGN, class E>
 AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int L = S.line.L, GL = S.GL;
   const int n1 = x.n1, c0 = it.c0, cn = it.cn;
   // block c0 / GL of region 1, laid out as this item's tile
-  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
+  const cx* blk = A.ws + x.ws + (i64)sdiv(c0, S.GLr) * x.s1;
   ex.phase_load([&](int tid) { copy_tables(tid, T, S, m); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk, x.s1);
   if (ex.failed) return;
-  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, S.GLr, cn);
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
     store_phase<T>(
         tid, L * GL, sk, x.off,
         [&](int u) {
-          const int k2 = u >> glogR, l = u & (GL - 1);
+          const int k2 = sdiv(u, S.GLr), l = u - k2 * GL;
           return l < cn ? c0 + l + n1 * k2 : -1;
         },
-        [&](int u) { return res[lpos(u >> glogR, u & (GL - 1), S.LS)]; }, loss);
+        [&](int u) {
+          const int k2 = sdiv(u, S.GLr);
+          return res[lpos(k2, u - k2 * GL, S.LS)];
+        },
+        loss);
   });
 }
 
@@ -750,7 +759,7 @@ AF_HD void rows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
 #pragma nv_exec_check_disable
 template <int T, int SIGN, class E>
 AF_HD cx* brows_spectrum(E& ex, const FShape& S, cx* sm, const FSmem& m, const FXform& x, int c0, int cn) {
-  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int L = S.line.L, GL = S.GL;
   const int M1 = x.n1;
   cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   cx* nxt = res == m.a ? m.b : m.a;
@@ -762,14 +771,14 @@ AF_HD cx* brows_spectrum(E& ex, const FShape& S, cx* sm, const FSmem& m, const F
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int u = u0 + r * T;
-        const int k2 = u >> glogR, l = u & (GL - 1);
+        const int k2 = sdiv(u, S.GLr), l = u - k2 * GL;
         sp[r] = (u < tot && l < cn) ? spec_at(x.spec, x.M, c0 + l + M1 * k2) : make_cx(0.f, 0.f);
       }
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int u = u0 + r * T;
         if (u < tot) {
-          const int k2 = u >> glogR, l = u & (GL - 1);
+          const int k2 = sdiv(u, S.GLr), l = u - k2 * GL;
           nxt[ipos(k2, l, GL)] = conjc(cmul_s<SIGN>(res[lpos(k2, l, S.LS)], sp[r]));
         }
       }
@@ -788,13 +797,13 @@ template <int T, int SIGN, class E>
 AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogR = ilog2i(GL);
+  const int L = S.line.L, GL = S.GL;
   const int M1 = x.n1, c0 = it.c0, cn = it.cn;
-  const cx* blk = A.ws + x.ws + (i64)(c0 >> glogR) * x.s1;
+  const cx* blk = A.ws + x.ws + (i64)sdiv(c0, S.GLr) * x.s1;
   ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
                 x.s1);
   if (ex.failed) return;
-  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, S.GLr, cn);
   cx* res;
   if (S.fixed) {
     // the spectrum product in the first FFT's last pass, written in the
@@ -805,13 +814,13 @@ AF_HD void brows_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, c
   } else {
     res = brows_spectrum<T, SIGN>(ex, S, sm, m, x, c0, cn);
   }
-  const int lga = ilog2i(x.ga);
   ex.phase([&](int tid) {
     for (int u = tid; u < cn * L; u += T) {
       const int l = (int)fdiv((unsigned)u, S.L1div);
       const int j2 = u - l * L;
       const int k1 = c0 + l;
-      A.ws[x.ws2 + (i64)(j2 >> lga) * x.s2 + k1 * x.ga + (j2 & (x.ga - 1))] =  // block j2 / ga
+      const int jb = sdiv(j2, x.gar);
+      A.ws[x.ws2 + (i64)jb * x.s2 + k1 * x.ga + (j2 - jb * x.ga)] =  // block j2 / ga
           cmul_s<SIGN>(res[lpos(j2, l, S.LS)], tl3<false>(m.wt3, (unsigned)(j2 * k1)));
     }
   });
@@ -824,25 +833,25 @@ template <int T, int SIGN, class E>
 AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, const FXform* xf, cx* sm) {
   const FSmem m = smem_of(S, sm);
   const FXform& x = xf[0];
-  const int L = S.line.L, GL = S.GL, glogC = ilog2i(GL);
+  const int L = S.line.L, GL = S.GL;
   const int M2 = x.n2, c0 = it.c0, cn = it.cn;
   // block c0 / GL of region 2, laid out as this item's tile
-  const cx* blk = A.ws + x.ws2 + (i64)(c0 >> glogC) * x.s2;
+  const cx* blk = A.ws + x.ws2 + (i64)sdiv(c0, S.GLr) * x.s2;
   ex.phase_load([&](int tid) { copy_multi_tables(tid, T, S, m, x); }, m.a, blk, (unsigned)(sizeof(cx) * L * GL), blk,
                 x.s2);
   if (ex.failed) return;
-  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, cn);
+  if (cn < GL) zero_lines<T>(ex, m.a, L, GL, S.GLr, cn);
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
   ex.phase_sum([&](int tid, float& loss) {
     store_phase<T>(
         tid, L * GL, sk, x.off,
         [&](int u) {
-          const int c = u & (GL - 1), j = (u >> glogC) * M2 + c0 + c;
+          const int j1 = sdiv(u, S.GLr), c = u - j1 * GL, j = j1 * M2 + c0 + c;
           return c < cn && j < x.n ? j : -1;
         },
         [&](int u) {
-          const int j1 = u >> glogC, c = u & (GL - 1);
+          const int j1 = sdiv(u, S.GLr), c = u - j1 * GL;
           return cmul_s<SIGN>(conjc(res[lpos(j1, c, S.LS)]), chirp_at<false>(x, m.ct3, j1 * M2 + c0 + c));
         },
         loss);

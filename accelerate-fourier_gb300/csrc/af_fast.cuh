@@ -200,13 +200,15 @@ AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, in
 // every stride, loop bound and divisor known to the compiler.
 // AFF_FIXED_LINES lists (L, GL, R1, R2): the lengths whose pairwise products
 // serve as the Bluestein convolution lengths of the multi-pass scheme, GL the
-// planner's line count for each under the default tuning.
+// planner's line count for each under the default tuning (as many lines as
+// fill a 4096-element item within the CTA's shared memory, at most 64; not
+// only powers of two: two lines share a unit only when GL is even).
 #define AFF_FIXED_LINES(X)                                                                                    \
-  X(64, 32, 16, 4) X(80, 32, 16, 5) X(96, 32, 16, 6) X(100, 32, 10, 10) X(120, 32, 15, 8) X(128, 32, 16, 8) \
-  X(144, 16, 16, 9) X(160, 16, 16, 10) X(180, 16, 15, 12) X(192, 16, 16, 12) X(200, 16, 20, 10)             \
-  X(216, 16, 24, 9) X(240, 16, 16, 15) X(250, 16, 25, 10) X(256, 16, 16, 16) X(270, 8, 27, 10)              \
-  X(288, 8, 32, 9) X(300, 8, 20, 15) X(320, 8, 16, 20) X(360, 8, 24, 15) X(384, 8, 32, 12) X(400, 8, 20, 20) \
-  X(432, 8, 27, 16) X(480, 8, 32, 15) X(500, 4, 25, 20) X(512, 4, 32, 16)
+  X(64, 64, 16, 4) X(80, 51, 16, 5) X(96, 42, 16, 6) X(100, 40, 10, 10) X(120, 34, 15, 8) X(128, 32, 16, 8) \
+  X(144, 28, 16, 9) X(160, 25, 16, 10) X(180, 22, 15, 12) X(192, 21, 16, 12) X(200, 20, 20, 10)             \
+  X(216, 18, 24, 9) X(240, 17, 16, 15) X(250, 16, 25, 10) X(256, 16, 16, 16) X(270, 15, 27, 10)              \
+  X(288, 14, 32, 9) X(300, 13, 20, 15) X(320, 12, 16, 20) X(360, 11, 24, 15) X(384, 10, 32, 12) X(400, 10, 20, 20) \
+  X(432, 9, 27, 16) X(480, 8, 32, 15) X(500, 7, 25, 20) X(512, 7, 32, 16)
 
 struct CRadices {
   int n;
@@ -342,7 +344,7 @@ AF_HD void cline_passes(E& ex, cx*& src, cx*& dst, const cx* tw, const LineEpi& 
   constexpr CRadices rs = c_radices(L);
   if constexpr (J < rs.n) {
     constexpr int R = rs.r[J], P = c_span(L, J), NB = L / R;
-    constexpr int V = (GL >= 2 && R <= 8) ? 2 : 1;
+    constexpr int V = (GL % 2 == 0 && R <= 8) ? 2 : 1;
     constexpr bool LAST = J == rs.n - 1;
     constexpr int LSo = LAST ? (L | 1) : 0;
     constexpr int TW = c_twoff(L, J);

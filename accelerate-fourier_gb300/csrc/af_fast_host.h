@@ -23,7 +23,8 @@ enum FKind {
 };
 
 // A shape: what every transform of an item shares.  The line FFT has length
-// L over GL interleaved lines;
+// L over GL interleaved lines (any GL for the compile-time lines, a power of
+// two for the others and for full-FFT shapes);
 // buffers hold `cap` elements each; LS is the line-major stride of the last
 // pass.  Full-FFT shapes (FK_DIRECT, FK_BLUE) have n = L*G with GL = Q*G
 // (Q transforms per CTA) and the final radix-G pass; multi-pass shapes have
@@ -40,6 +41,7 @@ struct FShape {
   int fixed;  // the line FFT is one of the compile-time lines (AFF_FIXED_LINES)
   int smem;  // shared-memory bytes an item of this shape uses
   FastDiv ndiv, L1div;
+  int GLr;        // ceil(2^19 / GL): x / GL = (x GLr) >> 19 for x < 8192 (sdiv)
   const cx* tw;   // pass twiddles (line.twn entries)
   const cx* ftw;  // final twiddles W_n^k1, k1 < L (ftwn entries)
 };
@@ -72,6 +74,7 @@ struct FXform {
   const cx* spec;  // Bluestein: spectrum FFT(b)/M of the conjugate chirp, entries 0..M/2
   unsigned n2x;    // Bluestein: 2n, the chirp's modulus
   float r2n;       // Bluestein: 1 / (2n) rounded to float
+  int gbr, gar;    // ceil(2^19 / gb), ceil(2^19 / ga) (sdiv)
 };
 
 struct FArgs {

@@ -200,9 +200,10 @@ struct FastBatch {
 
 // Every CTA of the persistent launch has 256 threads and the same shared
 // memory: three fit one SM (228 KB, less 1 KB reserved and the kernel's
-// 2.1 KB of staged descriptors and mbarrier per CTA).
+// 2.5 KB of staged descriptors and mbarrier per CTA).  The listed line counts
+// of the compile-time lines (AFF_FIXED_LINES) are those that fit this size.
 static const int kThreads = 256;
-static const int kCtaSmem = 74496;
+static const int kCtaSmem = 74240;
 static const int kMaxSmem = kCtaSmem;
 
 static size_t shape_smem(const FShape& s) {
@@ -239,7 +240,7 @@ static void choose_vectors(FShape& s, bool balance) {
     const i64 r1 = (u1 + kThreads - 1) / kThreads;
     const i64 r2 = (u1 / 2 + kThreads - 1) / kThreads;
     // a two-line unit costs about 1.7 one-line units
-    ps.V = (s.GL >= 2 && ps.R <= 8 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
+    ps.V = (s.GL % 2 == 0 && ps.R <= 8 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
     ps.glog = ilog2_up(s.GL / ps.V);
   }
 }
@@ -253,6 +254,7 @@ static void finish_shape(FShape& s, const FastTune& t) {
   s.aux = s.kind < 0 ? 1 : 0;
   s.ndiv = make_fastdiv((unsigned)s.n);
   s.L1div = make_fastdiv((unsigned)s.line.L);
+  s.GLr = (int)((1u << 19) + (unsigned)s.GL - 1) / s.GL;
   s.smem = (int)shape_smem(s);
   if (s.smem > kMaxSmem) throw FastError("shape of length " + std::to_string(s.n) + " needs too much shared memory");
 }
@@ -287,12 +289,19 @@ static int full_shape(FastBatch* B, int kind, i64 n, int Q) {
 
 // Line shape of the multi-pass schemes: FFT of length L over GL lines.
 static int line_shape(FastBatch* B, int L) {
-  // lines at most gl_max, GL * L at most the item target and within the
-  // shared memory of a CTA (two buffers of GL line-major rows)
+  auto fits = [&](int GL) {
+    return (i64)sizeof(cx) * (2 * even_up((i64)GL * (L | 1)) + 2 * L + 2 * AFF_TL3 + 16) <= kMaxSmem;
+  };
+  // A compile-time line takes as many lines as fill the item target within
+  // the shared memory of a CTA (two buffers of GL line-major rows), at most
+  // 64 (the listed pairs are these counts under the default tuning).  Other
+  // lines: a power of two, at most gl_max, GL * L at most the item target.
+  int GLf = (int)std::min<i64>(64, std::max<i64>(2, B->tune.target / L));
+  while (GLf > 2 && !fits(GLf)) --GLf;
+  const bool fixed_ok = B->tune.fixed && B->tune.radix16 && !B->tune.balance_v && is_fixed_line(L, GLf);
   int GL = B->tune.gl_max;
-  while (GL > 2 && ((i64)GL * L > B->tune.target ||
-                    (i64)sizeof(cx) * (2 * even_up((i64)GL * (L | 1)) + 2 * L + 2 * AFF_TL3 + 16) > kMaxSmem))
-    GL /= 2;
+  while (GL > 2 && ((i64)GL * L > B->tune.target || !fits(GL))) GL /= 2;
+  if (fixed_ok) GL = GLf;
   auto key = std::make_pair(L, GL);
   auto it = B->line_shapes.find(key);
   if (it != B->line_shapes.end()) return it->second;
@@ -527,8 +536,10 @@ static void plan_batch(FastBatch* B) {
     // holds (k1, j2) at k1 C1 + j2 mod C1.
     auto up16 = [](i64 v) { return (v + 15) & ~(i64)15; };
     x.gb = C2;
+    x.gbr = (int)((1u << 19) + (unsigned)C2 - 1) / C2;
     x.s1 = (int)up16(n2 * C2);
     x.ga = C1;
+    x.gar = (int)((1u << 19) + (unsigned)C1 - 1) / C1;
     x.s2 = blue ? (int)up16(n1 * C1) : 0;
     const i64 r1 = (n1 + C2 - 1) / C2 * x.s1;
     const i64 r2 = blue ? (n2 + C1 - 1) / C1 * x.s2 : 0;
