@@ -90,8 +90,9 @@ void gen_root_tables(const std::vector<RootSeg>& segs, cx* dbase, cx* hbase, cud
 __shared__ unsigned long long s_mbar;
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 #endif
-// polls of a bulk copy's mbarrier before the CTA reports FE_TIMEOUT
-#define AFF_BULK_POLLS (1ll << 24)
+// polls of a bulk copy's mbarrier before the CTA reports FE_TIMEOUT (a copy
+// completes within microseconds; 2^20 polls take tens of milliseconds at least)
+#define AFF_BULK_POLLS (1ll << 20)
 
 // Device: each phase is one call per thread followed by a barrier.
 struct DevExec {
@@ -297,11 +298,6 @@ AF_HD void store_phase(int tid, int total, const Sink& sk, i64 base, Idx idx, Va
   }
 }
 
-// x / d for 0 <= x < 8192 from r = ceil(2^19 / d), 2 <= d: exact when
-// d <= 64, since then x (r d - 2^19) < 8192 d <= 2^19, and for every power
-// of two (r d = 2^19); x r < 2^31.  One multiply and one shift.
-AF_HD int sdiv(int x, int r) { return (int)(((unsigned)x * (unsigned)r) >> 19); }
-
 // workspace element written by another CTA of this launch: read at L2 (no
 // stale L1 line)
 AF_HD cx ldws(const cx* p) {
@@ -410,8 +406,8 @@ AF_HD cx* line_fft(E& ex, const FShape& S, cx* src, cx* dst, const cx* tw, const
     const FPass ps = S.line.pass[j];
     const int LSo = j == np - 1 ? S.LS : 0;
     ex.phase([&](int tid) {
-      if (ps.V == 2) fpass_any<2, SIGN>(tid, T, src, dst, ps, S.GL, ps.glog, LSo, tw);
-      else fpass_any<1, SIGN>(tid, T, src, dst, ps, S.GL, ps.glog, LSo, tw);
+      if (ps.V == 2) fpass_any<2, SIGN>(tid, T, src, dst, ps, S.GL, S.GLr, LSo, tw);
+      else fpass_any<1, SIGN>(tid, T, src, dst, ps, S.GL, S.GLr, LSo, tw);
     });
     cx* t = src;
     src = dst;
@@ -521,7 +517,8 @@ AF_HD void load_contiguous(int tid, int T, cx* dst, const cx* src, int n) {
 // Lines [0, cn) of a strided matrix, rows e < L, into the interleaved layout
 // dst[e GL + c] = src[e stride + c]; lines cn..GL-1, and source positions
 // e stride + c >= lim, read as zero.  Pairs of lines move as 16-byte copies
-// at L2 when every pair is 16-byte aligned; otherwise one element at a time,
+// at L2 when GL is even and every pair is 16-byte aligned; otherwise one
+// element at a time,
 // at L2 for workspace sources (WS: written by other CTAs of this launch, so
 // never read through L1).
 // no limit on the source positions
@@ -674,7 +671,8 @@ AF_HD void blue_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, co
 
 // Multi-pass items work on one transform: columns [c0, c0 + cn) or lines
 // [c0, c0 + cn) of its n1 x n2 matrix (element (j1, j2) at j1 n2 + j2); the
-// shape's line FFT has GL lines (a power of two, cn <= GL).  The item stages
+// shape's line FFT has GL lines (cn <= GL; any count on a compile-time line,
+// else a power of two).  The item stages
 // the transform's three-level tables of W_N (wt) and W_2n (ct) with its loads.
 AF_HD void copy_multi_tables(int tid, int T, const FShape& S, const FSmem& m, const FXform& x) {
   copy_tables(tid, T, S, m);

@@ -32,13 +32,18 @@ namespace af {
 // writes q*p*R + k + m*p (k = b mod p, q = b div p) after the twiddles
 // W_{pR}^(k m), read from tw + (m-1)*p + k.
 // V: lines per unit of the pass (1 or 2, chosen so that the units spread
-// evenly over the CTA's threads); glog = log2(GL / V).
+// evenly over the CTA's threads; 2 only when the line count is even).
 struct FPass {
   int R, p, nb, tw;
   int plog;  // log2 p when p is a power of two, else -1
-  int V, glog;
+  int V;
   FastDiv pdiv;
 };
+
+// x / d for 0 <= x < 8192 from r = ceil(2^19 / d), 2 <= d: exact when
+// d <= 64, since then x (r d - 2^19) < 8192 d <= 2^19, and for every power
+// of two (r d = 2^19); x r < 2^31.  One multiply and one shift.
+AF_HD int sdiv(int x, int r) { return (int)(((unsigned)x * (unsigned)r) >> 19); }
 struct FLine {
   int L, npass, twn;  // length, passes, table entries
   FPass pass[AFF_MAXPASS];
@@ -165,28 +170,27 @@ AF_HD void fpass_unit(const cx* __restrict__ src, cx* __restrict__ dst, const FP
 
 // All units of one pass for thread `tid` of T (GL lines, V lines per unit).
 template <int R, int V, int SIGN>
-AF_HD void fpass_thread(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int glog, int LS,
+AF_HD void fpass_thread(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int gr, int LS,
                         const cx* tw) {
-  const int units = ps.nb << glog;
-  const int gmask = (1 << glog) - 1;
+  const int units = ps.nb * (GL / V);
   for (int u = tid; u < units; u += T) {
-    const int b = u >> glog;
-    const int line = (u & gmask) * V;
+    const int b = sdiv(u * V, gr);  // unit u: butterfly b of lines (u mod GL/V) V ..
+    const int line = u * V - b * GL;
     fpass_unit<R, V, SIGN>(src, dst, ps, b, line, GL, LS, tw);
   }
 }
 
 template <int V, int SIGN>
-AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int glog, int LS,
+AF_HD void fpass_any(int tid, int T, const cx* src, cx* dst, const FPass& ps, int GL, int gr, int LS,
                      const cx* tw) {
   switch (ps.R) {
-    case 2: fpass_thread<2, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
-    case 3: fpass_thread<3, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
-    case 4: fpass_thread<4, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
-    case 5: fpass_thread<5, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
-    case 8: fpass_thread<8, V, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw); break;
+    case 2: fpass_thread<2, V, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw); break;
+    case 3: fpass_thread<3, V, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw); break;
+    case 4: fpass_thread<4, V, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw); break;
+    case 5: fpass_thread<5, V, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw); break;
+    case 8: fpass_thread<8, V, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw); break;
     default:  // 16: one line per unit (the planner never pairs lines at radix 16)
-      if (V == 1) fpass_thread<16, 1, SIGN>(tid, T, src, dst, ps, GL, glog, LS, tw);
+      if (V == 1) fpass_thread<16, 1, SIGN>(tid, T, src, dst, ps, GL, gr, LS, tw);
       break;
   }
 }

@@ -224,12 +224,6 @@ static i64 table_tl3(FastBatch* B, i64 N) {
   return off;
 }
 
-static int ilog2_up(int v) {
-  int l = 0;
-  while ((1 << l) < v) ++l;
-  return l;
-}
-
 // Lines per unit of each pass: two lines share the twiddle loads and move as
 // 16-byte vectors, but one line per unit wins when it spreads the units
 // over the threads in fewer rounds.
@@ -241,7 +235,6 @@ static void choose_vectors(FShape& s, bool balance) {
     const i64 r2 = (u1 / 2 + kThreads - 1) / kThreads;
     // a two-line unit costs about 1.7 one-line units
     ps.V = (s.GL % 2 == 0 && ps.R <= 8 && (!balance || 2 * r2 * 17 <= r1 * 20)) ? 2 : 1;
-    ps.glog = ilog2_up(s.GL / ps.V);
   }
 }
 
@@ -292,16 +285,22 @@ static int line_shape(FastBatch* B, int L) {
   auto fits = [&](int GL) {
     return (i64)sizeof(cx) * (2 * even_up((i64)GL * (L | 1)) + 2 * L + 2 * AFF_TL3 + 16) <= kMaxSmem;
   };
-  // A compile-time line takes as many lines as fill the item target within
-  // the shared memory of a CTA (two buffers of GL line-major rows), at most
-  // 64 (the listed pairs are these counts under the default tuning).  Other
-  // lines: a power of two, at most gl_max, GL * L at most the item target.
-  int GLf = (int)std::min<i64>(64, std::max<i64>(2, B->tune.target / L));
-  while (GLf > 2 && !fits(GLf)) --GLf;
+  // As many lines as fill the item target within the shared memory of a CTA
+  // (two buffers of GL line-major rows): at most 64 on a compile-time line
+  // (the listed pairs are these counts under the default tuning), at most
+  // gl_max and 64 on the others (the item code divides by the line count
+  // with a reciprocal that is exact up to 64).
+  // (a tile of L GL elements moves as one bulk copy, whose size must be a
+  // multiple of 16 bytes: an odd L takes an even count)
+  auto fill = [&](int cap) {
+    int g = (int)std::min<i64>(cap, std::max<i64>(2, B->tune.target / L));
+    while (g > 2 && (!fits(g) || (L & g & 1))) --g;
+    return g;
+  };
+  const int GLf = fill(64);
   const bool fixed_ok = B->tune.fixed && B->tune.radix16 && !B->tune.balance_v && is_fixed_line(L, GLf);
-  int GL = B->tune.gl_max;
-  while (GL > 2 && ((i64)GL * L > B->tune.target || !fits(GL))) GL /= 2;
-  if (fixed_ok) GL = GLf;
+  const int GL = fixed_ok ? GLf : fill(std::min(B->tune.gl_max, 64));
+  if (((i64)L * GL) % 2 != 0) throw FastError("a tile of an odd number of elements cannot move as one bulk copy");
   auto key = std::make_pair(L, GL);
   auto it = B->line_shapes.find(key);
   if (it != B->line_shapes.end()) return it->second;

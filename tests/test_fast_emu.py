@@ -154,3 +154,19 @@ def test_no_wait_to_poison_in_single_stage_batches():
     assert e.L.afx_fast_poison_wait(e.h, 1000) == 1
     e.run(np.ones(164, dtype=np.complex64), -1)
     assert e.status() == 0
+
+
+def test_odd_lines_take_even_tiles():
+    # 6561 = 81 x 81 and 50625 = 225 x 225 run four-step over odd line
+    # lengths; with 3072-element items of up to 64 lines the planner would take 37 and 13
+    # lines, tiles of an odd number of elements that cannot move as one bulk
+    # copy: it takes an even count instead
+    sizes = [6561, 50625]
+    rng = np.random.default_rng(23)
+    x = crand(rng, int(np.sum(sizes)), "normal")
+    t = np.array([1, 64, 0, 3072, 2736, 48], dtype=np.int32)
+    e = Emu(sizes, tune=t)
+    assert e.describe()["by_kind"][2] > 0
+    y, _ = e.run(x, -1)
+    for n, xi, yi in zip(sizes, split(x, sizes), split(y, sizes)):
+        assert rel_l2(yi, np.fft.fft(xi)) <= fp32_bound(n, 4.0), n
