@@ -841,9 +841,12 @@ AF_HD void bcols2_item(E& ex, const FArgs& A, const FItem& it, const FShape& S, 
   if (cn < GL) zero_lines<T>(ex, m.a, L, GL, S.GLr, cn);
   const cx* res = run_line<T, SIGN>(ex, S, sm, m.a, m.b, m.tw);
   const Sink sk{A.out, A.w};
+  // rows j1 >= ceil((n - c0) / M2) fall past the transform's n outputs
+  const i64 rr = ((i64)x.n - c0 + M2 - 1) / M2;
+  const int rows = rr < L ? (int)rr : L;
   ex.phase_sum([&](int tid, float& loss) {
     store_phase<T>(
-        tid, L * GL, sk, x.off,
+        tid, rows * GL, sk, x.off,
         [&](int u) {
           const int j1 = sdiv(u, S.GLr), c = u - j1 * GL, j = j1 * M2 + c0 + c;
           return c < cn && j < x.n ? j : -1;
