@@ -845,8 +845,9 @@ int fast_status(FastBatch* B, cudaStream_t st);
 
 // ------------------------------------------------------------ autotuner
 // The planner's choices are timed on the device for the batch at hand: from
-// the defaults, each choice in turn (stage slack, lines per multi-pass item,
-// radix-16 passes with the compile-time lines, item size) takes the value
+// the defaults, each choice in turn (stage slack, workspace in flight, lines
+// per multi-pass item, radix-16 passes with the compile-time lines, item
+// size) takes the value
 // with the shortest forward launch, the others held.  Operation counts do
 // not predict the time (the reference's planner says as much of its own
 // algorithm choice, Planned.hs:206-214); the launch is timed with CUDA events,
@@ -990,7 +991,7 @@ FastBatch* fast_create_tuned(const i64* ns, i64 count, const char* cache_path, c
     const struct {
       int field;
       std::vector<int> values;
-    } axes[] = {{4, {1368, 5472}}, {1, {16, 64}}, {0, {0}}, {3, {3072}}};
+    } axes[] = {{4, {1368, 5472}}, {5, {24, 96}}, {1, {16, 64}}, {0, {0}}, {3, {3072}}};
     for (const auto& ax : axes)
       for (int val : ax.values) {
         int cand[kTuneFields];
